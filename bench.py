@@ -1,0 +1,445 @@
+#!/usr/bin/env python
+"""EFF forward + both adjoints throughput on GB300 (one JSON line).
+
+Workload (default ``cfg2``): one 512x512 float32 blob+edge image cut into an
+8x8 grid of 96x96 patches at 50% overlap (hop 48), 128x128 FFT frame, one
+31x31 random-walk motion PSF per patch; ``y_obs = EFF(x, f) + N(0, 0.01^2)``.
+One step is the autograd step of ``0.5*||EFF(x, f) - y_obs||^2``: PSF
+spectrum, fused forward (which also leaves the windowed-patch spectrum),
+residual, fused adjoint giving both gradients.  Metric: image Mpixel/s of
+that step.  Inputs are seeded synthetic data (no dataset is distributed).
+
+``value``: device-resident inputs, the step captured in a CUDA graph, L2
+flushed (256 MB write) before every timed step, per-step CUDA events summed.
+``e2e``: the same step through the public API from pinned host buffers, with
+the host->device copy of (x, f, y_obs) and the device->host copy of
+(gx, gf, loss) inside the timed region.
+``--impl reference``: the FP64 oracle port of the reference algorithm on the
+host cores (scipy.fft over all cores), same workload.
+
+Multi-GPU (``torchrun``): every rank runs its own image (replicas, weak
+scaling, no collective in the data path); value = images of all ranks / max
+rank time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    "cfg2": dict(desc="512x512, 8x8 grid of 96x96 patches (hop 48), 31x31 motion PSFs, frame 128",
+                 sx=(512, 512), csf=(8, 8), sf=(31, 31), sw=(96, 96), hop=(48, 48), kind="motion"),
+    "cfg2_winaux": dict(desc="512x512, 8x8 grid, win2winaux patches 122x122 (hop 61), 31x31 motion PSFs, frame 256",
+                        sx=(512, 512), csf=(8, 8), sf=(31, 31), sw=None, hop=None, kind="motion"),
+    "cfg1": dict(desc="256x256, 4x4 grid of 64x64 patches (hop 32), 15x15 Gaussian PSFs, frame 128",
+                 sx=(256, 256), csf=(4, 4), sf=(15, 15), sw=(64, 64), hop=(32, 32), kind="gauss"),
+}
+FLUSH_BYTES = 256 << 20
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured", float(d.get("sm_max_mhz", 2070.0))
+    return 6800.0, "fallback", 2070.0
+
+
+def make_inputs(w, seed):
+    from vmbd_gb300 import geometry, synth
+    wa = geometry.win2winaux(w["sx"], w["csf"], 0.5, sw=w["sw"], nhop=w["hop"])
+    x = synth.blob_edge_image(w["sx"], seed=seed)
+    gen = synth.motion_psfs if w["kind"] == "motion" else synth.gaussian_psfs
+    f = gen(wa.K, w["sf"], seed=seed + 1000)
+    return wa, x, f
+
+
+def algorithmic(w, wa, N):
+    """Unique fp32 I/O bytes and reference-algorithm FFT flops per image."""
+    sx, sf, K = w["sx"], w["sf"], wa.K
+    sy = (sx[0] - sf[0] + 1, sx[1] - sf[1] + 1)
+    px, pf, py = sx[0] * sx[1] * 4, K * sf[0] * sf[1] * 4, sy[0] * sy[1] * 4
+    fft = 5.0 * N * N * np.log2(N * N)  # one complex 2-D FFT, benchFFT convention
+    prod = 6.0 * N * N
+    return {
+        # forward y = F x: reads x and f, writes y; 3K FFTs + K products
+        "forward": (px + pf + py, K * (3 * fft + prod)),
+        # both adjoints: reads r, x, f, writes gx and gf; 4K FFTs + 2K products
+        "adjoint": (py + px + pf + px + pf, K * (4 * fft + 2 * prod)),
+        "psf_spectrum": (pf + K * (N // 2 + 1) * N * 8, K * fft),
+    }
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            p = [s.strip() for s in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx.append(float(p[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def run_ours(args, rank, world, dev):
+    import torch
+    from vmbd_gb300.eff import EffPlan
+
+    w = WORKLOADS[args.workload]
+    wa, x_np, f_np = make_inputs(w, seed=rank)
+    plan = EffPlan(wa, w["sf"], "valid", device=dev)
+    N, K = plan.N, plan.K
+    x = torch.from_numpy(x_np).to(dev)
+    f = torch.from_numpy(f_np).to(dev)
+    gen = torch.Generator(device=dev).manual_seed(1234 + rank)
+    y_obs = plan.forward_image(x, plan.psf_spectrum(f))
+    y_obs += 0.01 * torch.randn(y_obs.shape, device=dev, generator=gen)
+
+    # static buffers of the step
+    fhat = plan.empty_spectrum()
+    xhat = plan.empty_spectrum()
+    y = torch.empty(plan.sy, device=dev)
+    r = torch.empty(plan.sy, device=dev)
+    gx = torch.empty(plan.sx, device=dev)
+    gf = torch.empty((K,) + plan.sf, device=dev)
+    loss = torch.empty((), device=dev)
+
+    def step():
+        plan.psf_spectrum(f, out=fhat)
+        plan.forward_image(x, fhat, out=y, xhat_out=xhat)
+        torch.sub(y, y_obs, out=r)
+        torch.mul(0.5, torch.sum(r * r), out=loss)
+        plan.adjoint(r, fhat, xhat, gx=gx, gf=gf)
+
+    flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    with torch.cuda.stream(stream):
+        for _ in range(3):
+            step()
+        torch.cuda.synchronize(dev)
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph, stream=stream):
+            step()
+        torch.cuda.synchronize(dev)
+
+        def timed_graph(n):
+            evs = []
+            for _ in range(n):
+                flush.fill_(1.0)
+                a = torch.cuda.Event(enable_timing=True)
+                b = torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                graph.replay()
+                b.record(stream)
+                evs.append((a, b))
+            torch.cuda.synchronize(dev)
+            return sum(a.elapsed_time(b) for a, b in evs)
+
+        timed_graph(args.warmup)
+        clocks = Clocks(dev.index if dev.index is not None else 0)
+        barrier(world)
+        torch.cuda.synchronize(dev)
+        clocks.start()
+        t_ms = timed_graph(args.steps)
+        torch.cuda.synchronize(dev)
+        barrier(world)
+        clk = clocks.stop()
+        t_ms = allreduce_max(t_ms, world, dev)
+
+        # per-kernel durations (eager launches, L2 flushed before each step)
+        names = ["psf_spectrum", "forward", "residual", "adjoint"]
+        acc = {n: 0.0 for n in names}
+        reps = max(5, min(args.steps, 50))
+        for _ in range(reps):
+            flush.fill_(1.0)
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
+            ev[0].record(stream)
+            plan.psf_spectrum(f, out=fhat)
+            ev[1].record(stream)
+            plan.forward_image(x, fhat, out=y, xhat_out=xhat)
+            ev[2].record(stream)
+            torch.sub(y, y_obs, out=r)
+            torch.mul(0.5, torch.sum(r * r), out=loss)
+            ev[3].record(stream)
+            plan.adjoint(r, fhat, xhat, gx=gx, gf=gf)
+            ev[4].record(stream)
+            torch.cuda.synchronize(dev)
+            for i, n in enumerate(names):
+                acc[n] += ev[i].elapsed_time(ev[i + 1])
+        kern_ms = {n: acc[n] / reps for n in names}
+
+        # unfused per-stage comparator (torch ops + cuFFT), graph-captured
+        from vmbd_gb300.unfused import UnfusedEff
+        U = UnfusedEff(wa, w["sf"], N=N, device=dev)
+
+        def ustep():
+            fh = U.psf_spectrum(f)
+            yy, xh = U.forward(x, fh)
+            rr = yy - y_obs
+            U.adjoint(rr, fh, xh)
+            return 0.5 * (rr * rr).sum()
+
+        for _ in range(3):
+            ustep()
+        torch.cuda.synchronize(dev)
+        ug = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(ug, stream=stream):
+            ustep()
+        torch.cuda.synchronize(dev)
+        ut = 0.0
+        for i in range(args.warmup + args.steps):
+            flush.fill_(1.0)
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            ug.replay()
+            b.record(stream)
+            torch.cuda.synchronize(dev)
+            if i >= args.warmup:
+                ut += a.elapsed_time(b)
+        unfused_ms = ut / args.steps
+
+        # end to end through the public API from pinned host buffers
+        hx = torch.from_numpy(x_np).pin_memory()
+        hf = torch.from_numpy(f_np).pin_memory()
+        hy = y_obs.cpu().pin_memory()
+        ogx = torch.empty(plan.sx).pin_memory()
+        ogf = torch.empty((K,) + plan.sf).pin_memory()
+        oloss = torch.empty(()).pin_memory()
+
+        def e2e_step():
+            x.copy_(hx, non_blocking=True)
+            f.copy_(hf, non_blocking=True)
+            y_obs.copy_(hy, non_blocking=True)
+            graph.replay()
+            ogx.copy_(gx, non_blocking=True)
+            ogf.copy_(gf, non_blocking=True)
+            oloss.copy_(loss, non_blocking=True)
+
+        for _ in range(args.warmup):
+            e2e_step()
+        torch.cuda.synchronize(dev)
+        et = 0.0
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            e2e_step()
+            b.record(stream)
+            torch.cuda.synchronize(dev)
+            et += a.elapsed_time(b)
+        et = allreduce_max(et, world, dev)
+    h2d = (hx.numel() + hf.numel() + hy.numel()) * 4
+    d2h = (ogx.numel() + ogf.numel()) * 4 + 4
+    return dict(plan=plan, wa=wa, w=w, x_np=x_np, f_np=f_np, y_obs=y_obs.cpu().numpy(),
+                gx=gx.cpu().numpy(), gf=gf.cpu().numpy(), y=y.cpu().numpy(), t_ms=t_ms,
+                kern_ms=kern_ms, unfused_ms=unfused_ms, e2e_ms=et, h2d=h2d, d2h=d2h, clocks=clk)
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allreduce_max(v, world, dev):
+    if world <= 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def oracle_step(w, wa, x, f, y_obs):
+    """One fwd + both exact adjoints of the FP64 oracle."""
+    from oracle import eff64
+    g = eff64.Geometry(w["sx"], w["sf"], wa.csf, wa.sw, wa.nhop, "valid")
+    ws = wa.ws.astype(np.float64)
+    y = eff64.forward(x, f, g, ws)
+    r = y - y_obs
+    return y, eff64.adjoint_image(r, f, g, ws), eff64.adjoint_psf(r, x, g, ws)
+
+
+def cpu_sample(w, wa, x, f, y_obs, budget_s=12.0, max_reps=50, warm=1):
+    """Time the oracle step on the host (scipy.fft over all cores)."""
+    from oracle import eff64
+    cores = os.cpu_count() or 1
+    eff64.set_fft_workers(cores)
+    for _ in range(warm):
+        oracle_step(w, wa, x, f, y_obs)
+    times, out = [], None
+    t_end = time.perf_counter() + budget_s
+    while len(times) < max_reps and (not times or time.perf_counter() < t_end):
+        t0 = time.perf_counter()
+        out = oracle_step(w, wa, x, f, y_obs)
+        times.append(time.perf_counter() - t0)
+    return statistics.median(times), len(times), cores, out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=list(WORKLOADS), default="cfg2")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    w = WORKLOADS[args.workload]
+    pixels = w["sx"][0] * w["sx"][1]
+    metric = "EFF fwd+adjoint Mpixel/s"
+    config = {"workload": args.workload, "desc": w["desc"], "step": "psf spectrum + fused forward + "
+              "residual/loss + fused adjoint (both gradients)", "images_per_gpu": 1,
+              "l2": "flushed (256 MB write) before every timed step", "parallelism": f"replicas x{world}"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        from vmbd_gb300 import geometry  # noqa: F401
+        wa, x, f = make_inputs(w, seed=0)
+        from oracle import eff64
+        g = eff64.Geometry(w["sx"], w["sf"], wa.csf, wa.sw, wa.nhop, "valid")
+        y_obs = eff64.forward(x, f, g, wa.ws.astype(np.float64))
+        y_obs = y_obs + 0.01 * np.random.default_rng(1234).standard_normal(y_obs.shape)
+        cores = os.cpu_count() or 1
+        eff64.set_fft_workers(cores)
+        for _ in range(args.warmup):
+            oracle_step(w, wa, x, f, y_obs)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            oracle_step(w, wa, x, f, y_obs)
+        dt = (time.perf_counter() - t0) / args.steps
+        v = pixels / dt / 1e6
+        print(json.dumps({
+            "impl": "reference", "metric": metric, "value": v, "unit": "Mpixel/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config,
+            "cpu_baseline": {"value": v, "unit": "Mpixel/s", "cores": cores, "kind": "port",
+                             "sample": "one full image per step (FP64 NumPy oracle of the reference "
+                                       "algorithm, scipy.fft over all host cores)"},
+            "e2e": {"value": v, "unit": "Mpixel/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }))
+        return
+
+    import torch
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    R = run_ours(args, rank, world, dev)
+    plan, wa = R["plan"], R["wa"]
+    ms = R["t_ms"] / args.steps
+    value = world * pixels / (ms * 1e-3) / 1e6
+    e2e_ms = R["e2e_ms"] / args.steps
+    hbm, hbm_kind, sm_max = peaks()
+    alg = algorithmic(w, wa, plan.N)
+    kern = {k: v for k, v in R["kern_ms"].items() if k in alg}
+    dom = max(kern, key=kern.get)
+    bytes_, flops = alg[dom]
+    t_dom = kern[dom] * 1e-3
+    achieved = bytes_ / t_dom / 1e9
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", f"traffic_{args.workload}.json")
+    if os.path.exists(tp):
+        traffic = json.load(open(tp)).get(dom)
+    clk = R["clocks"]
+    sm_mhz = clk["sm_mhz"] if clk else sm_max
+    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+    line = {
+        "metric": metric, "value": value, "unit": "Mpixel/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded blob+edge image, motion PSFs)",
+        "config": config,
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm,
+                     "peak_kind": hbm_kind, "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic,
+                     "algorithmic_bytes": bytes_, "kernel_ms": kern[dom],
+                     "fp32": {"ref_alg_tflops": flops / t_dom / 1e12, "peak_tflops_at_clock": fp32_peak,
+                              "frac": flops / t_dom / 1e12 / fp32_peak}},
+        "kernels_ms": R["kern_ms"],
+        "unfused_gpu": {"ms_per_step": R["unfused_ms"], "value": world * pixels / (R["unfused_ms"] * 1e-3) / 1e6,
+                        "speedup": R["unfused_ms"] / ms},
+        "e2e": {"value": world * pixels / (e2e_ms * 1e-3) / 1e6, "unit": "Mpixel/s",
+                "ms_per_step": e2e_ms, "h2d_bytes_per_step": R["h2d"], "d2h_bytes_per_step": R["d2h"]},
+        "gpu_launches": 3 * args.steps,
+        "clocks": clk,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        t_cpu, reps, cores, (y_o, gx_o, gf_o) = cpu_sample(w, wa, R["x_np"], R["f_np"], R["y_obs"])
+        line["cpu_baseline"] = {"value": pixels / t_cpu / 1e6, "unit": "Mpixel/s", "cores": cores,
+                                "kind": "port",
+                                "sample": f"{reps} full-image steps of the same workload (FP64 NumPy "
+                                          f"oracle, scipy.fft over {cores} cores), median"}
+
+        def rel(a, b):
+            return float(np.linalg.norm(np.asarray(a, np.float64) - b) / np.linalg.norm(b))
+        line["rel_l2_vs_fp64_oracle"] = {"forward": rel(R["y"], y_o), "adjoint_image": rel(R["gx"], gx_o),
+                                         "adjoint_psf": rel(R["gf"], gf_o)}
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

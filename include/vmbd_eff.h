@@ -1,0 +1,118 @@
+/* vmbd_eff.h -- C ABI of the GB300 efficient-filter-flow (EFF) operator.
+ *
+ * Drop-in for the device work behind VMBD's OlaGPU class (olaGPU.py) and its
+ * gputools wrappers.  All data pointers are caller-owned DEVICE pointers
+ * (float32, C order); `stream` is a cudaStream_t passed as void* (NULL = the
+ * legacy default stream).  Every entry point returns an EFF_* status and
+ * never aborts; eff_last_error() describes the last failure on the calling
+ * thread.  Plans are immutable after creation and may be used from several
+ * host threads / streams at once.  The compute entry points allocate nothing.
+ *
+ * Geometry (per dim d): image sx, PSF sf, patch grid csf, patch size sw,
+ * hop; K = csf0*csf1 patches, patch k = m*csf1 + n at (m*hop0, n*hop1);
+ * E = sw + sf - 1; output size sy = sx-sf+1 (valid), sx (same), sx+sf-1
+ * (full).
+ *
+ * Window stack (win2winaux, imagetools.py:398-454): the partition of unity
+ * ws = w / chop(ola(w)) of a separable window w floored at 1e-16 is passed as
+ * two per-dim tables of float pairs, win0 [csf0][sw0][2] and
+ * win1 [csf1][sw1][2], entry (alpha, gamma) for patch row m (column n) and
+ * local row r (column c) with global coordinate i = m*hop + r:
+ *   alpha = a[r] / sum over covering patches m' of a[i - m'*hop]
+ *           (a = the 1-D window scaled to max 1), or -1 when every covering
+ *           patch has a zero window sample at i (the outermost rows);
+ *   gamma = 1 / (number of patches covering i).
+ * ws[k][r][c] = alpha0*alpha1 when both alphas are >= 0, else gamma0*gamma1.
+ *
+ * Batched calls run `batch` images of the same geometry, stored back to
+ * back (image stride = the per-image size of each array).
+ */
+#ifndef VMBD_EFF_H
+#define VMBD_EFF_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define EFF_OK 0
+#define EFF_ERR_INVALID 1     /* bad argument: null pointer, inconsistent geometry */
+#define EFF_ERR_UNSUPPORTED 2 /* geometry outside what the kernels handle */
+#define EFF_ERR_CUDA 3        /* a CUDA runtime call failed */
+
+#define EFF_MODE_VALID 0
+#define EFF_MODE_SAME 1
+#define EFF_MODE_FULL 2
+
+#define EFF_ADJ_EXACT 0     /* exact transpose of the forward operator */
+#define EFF_ADJ_REFERENCE 1 /* OlaGPU.cnvtp's truncated chop (olaGPU.py:276-286) */
+
+typedef struct EffGeom {
+  int sx[2];   /* image size */
+  int sf[2];   /* PSF size */
+  int csf[2];  /* patch grid */
+  int sw[2];   /* patch size */
+  int hop[2];  /* patch hop */
+  int sfft;    /* FFT frame edge: 0 = smallest power of two >= max(E) (>= 64) */
+  int mode;    /* EFF_MODE_* */
+} EffGeom;
+
+typedef struct EffPlan EffPlan;
+
+/* Replaces OlaGPU.__init__'s geometry checks (olaGPU.py:95-168) and the
+ * window upload of win2winaux (imagetools.py:437-454).  win0 [csf0*sw0*2] and
+ * win1 [csf1*sw1*2] are HOST arrays; the plan keeps device copies. */
+int eff_plan_create(const EffGeom* geom, const float* win0, const float* win1, EffPlan** plan);
+int eff_plan_destroy(EffPlan* plan);
+
+/* FFT frame edge chosen by the plan, and the bytes of one image's cached
+ * spectrum (K * (N/2+1) * N complex64). */
+int eff_plan_frame(const EffPlan* plan, int* n);
+size_t eff_spectrum_bytes(const EffPlan* plan);
+
+/* PSF spectrum cache of an F object: pad_stack_GPU + FFT, olaGPU.py:142-157.
+ * f [batch, K, sf0, sf1] -> fhat [batch, spectrum]. */
+int eff_psf_spectrum(const EffPlan* plan, const float* f, void* fhat, int batch, void* stream);
+
+/* Windowed-patch spectrum cache of an X object: chop_mod_pad_GPU + FFT,
+ * olaGPU.py:147-157.  x [batch, sx0, sx1] -> xhat. */
+int eff_image_spectrum(const EffPlan* plan, const float* x, void* xhat, int batch, void* stream);
+
+/* F.cnv(x), olaGPU.py:170-257: y = crop(OLA(IFFT(fhat * FFT(ws * chop(x))))).
+ * y [batch, sy0, sy1] is overwritten.  xhat_out (nullable) receives the
+ * windowed-patch spectrum of x as eff_image_spectrum would. */
+int eff_forward_image(const EffPlan* plan, const float* x, const void* fhat, float* y,
+                      void* xhat_out, int batch, void* stream);
+
+/* X.cnv(f), olaGPU.py:170-257 with the X object: same operator, the PSFs
+ * transformed in-kernel.  fhat_out (nullable) receives f's spectrum. */
+int eff_forward_psf(const EffPlan* plan, const float* f, const void* xhat, float* y,
+                    void* fhat_out, int batch, void* stream);
+
+/* F.cnvtp(y) and X.cnvtp(y), olaGPU.py:261-311, sharing one transform of y.
+ * gx [batch, sx0, sx1] (needs fhat) and/or gf [batch, K, sf0, sf1] (needs
+ * xhat) are overwritten; pass NULL for an output that is not wanted.
+ * adj_mode: EFF_ADJ_EXACT or EFF_ADJ_REFERENCE. */
+int eff_adjoint(const EffPlan* plan, const float* y, const void* fhat, const void* xhat, float* gx,
+                float* gf, int adj_mode, int batch, void* stream);
+
+/* PSF projections on [K, n] stacks (n = sf0*sf1), in place.
+ * EFF_PROJ_CLIP_NORMALIZE: f = max(f, 0) then f /= sum(f) when sum > 1e-6
+ *   (L-BFGS-B bounds olaGPU.py:404-411 + normalize gputools.py:1025-1044).
+ * EFF_PROJ_SIMPLEX: Euclidean projection onto {f >= 0, sum f = 1}. */
+#define EFF_PROJ_CLIP_NORMALIZE 0
+#define EFF_PROJ_SIMPLEX 1
+int eff_project_psf(float* f, int K, int n, int proj_mode, void* stream);
+
+/* projection.cu:3-27 as intended: w[b] = <fs, basis[b]> for b < nb, with
+ * fs [n] and basis [nb, n]. */
+int eff_basis_project(const float* fs, const float* basis, float* w, int nb, int n, void* stream);
+
+/* Message for the last non-OK status returned on this thread. */
+const char* eff_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VMBD_EFF_H */

@@ -1,0 +1,84 @@
+"""Generate the golden EFF fixtures in this directory from the reference.
+
+Runs the reference's own ``win2winaux``, ``OlaGPU.__init__/cnv/cnvtp`` and
+``gputools`` wrappers over its ``gputools.cu`` kernels compiled for the CPU
+(``oracle/ref_harness.py``; pyfft replaced by a complex64 numpy FFT), in FP32
+as the reference computes, on small seeded cases, and stores inputs and
+outputs as ``ref_<case>.npz``.
+
+Entries the reference leaves undefined are stored as NaN: where the patch grid
+covers less than the image, ``crop_gpu2cpu`` reads beyond the overlap-added
+array (no source bounds check in crop_Kernel, gputools.cu:254-263).
+
+Needs the reference checkout; run ``python tests/golden/make_golden.py``.
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+
+from oracle import ref_harness as rh  # noqa: E402
+from vmbd_gb300 import synth  # noqa: E402
+
+# name: (sx, csf, sf, mode, winaux_sx (None: the image size), psf kind, seed)
+CASES = {
+    "valid_mixed_parity": ((60, 52), (3, 2), (7, 5), "valid", None, "gauss", 11),
+    "literal_uncovered": ((64, 64), (2, 2), (9, 9), "valid", (36, 36), "motion", 12),
+    "same_even_psf": ((50, 70), (2, 3), (6, 8), "same", None, "gauss", 13),
+    "grid4x4_sf15": ((96, 96), (4, 4), (15, 15), "valid", None, "gauss", 14),
+    "wide_nonsquare": ((40, 120), (2, 5), (5, 11), "valid", None, "motion", 15),
+}
+
+
+def make_case(name, sx, csf, sf, mode, wa_sx, kind, seed, gputools, imagetools, olaGPU):
+    sx = np.array(sx)
+    sf = np.array(sf)
+    K = int(np.prod(csf))
+    wa = imagetools.win2winaux(np.array(wa_sx if wa_sx else sx), csf, 0.5)
+    wa.sx = sx  # literal geometry: the window stack of a smaller grid on this image
+    x = synth.blob_edge_image(tuple(sx), seed=seed)
+    gen = synth.gaussian_psfs if kind == "gauss" else synth.motion_psfs
+    f = gen(K, tuple(sf), seed=seed + 100)
+
+    F = olaGPU.OlaGPU(f, sx, mode, wa)
+    y = F.cnv(x)
+    X = olaGPU.OlaGPU(rh.cua.to_gpu(x), sf, mode, wa)
+    yX = X.cnv(f)
+    r = np.random.default_rng(seed + 200).standard_normal(y.shape).astype(np.float32)
+    gx = F.cnvtp(rh.cua.to_gpu(r)).get()
+    gf = X.cnvtp(rh.cua.to_gpu(r)).get()
+
+    sw = np.array(wa.sw, dtype=int)
+    hop = np.array(wa.nhop, dtype=int)
+    sxp = hop * np.array(csf) + sw - hop
+    off = {"valid": sf - 1, "same": sf // 2, "full": 0 * sf}[mode]
+    yfull = sxp + sf - 1
+    ii, jj = np.meshgrid(np.arange(y.shape[0]), np.arange(y.shape[1]), indexing="ij")
+    undefined_y = (ii + off[0] >= yfull[0]) | (jj + off[1] >= yfull[1])
+    ii, jj = np.meshgrid(np.arange(sx[0]), np.arange(sx[1]), indexing="ij")
+    undefined_x = (ii >= sxp[0]) | (jj >= sxp[1])
+    for a, m in ((y, undefined_y), (yX, undefined_y), (gx, undefined_x)):
+        a[m] = np.nan
+    out = dict(sx=sx, sf=sf, csf=np.array(csf), sw=sw, hop=hop, mode=np.array(mode),
+               sfft=np.array(F.sfft_gpu), x=x, f=f, r=r,
+               ws=np.asarray(wa.ws_gpu, np.float32), y=y.astype(np.float32),
+               yX=yX.astype(np.float32), gx=gx.astype(np.float32), gf=gf.astype(np.float32))
+    path = os.path.join(HERE, f"ref_{name}.npz")
+    np.savez_compressed(path, **out)
+    print(f"{name}: sx={tuple(sx)} csf={csf} sf={tuple(sf)} sw={tuple(sw)} hop={tuple(hop)} "
+          f"sfft={F.sfft_gpu} mode={mode} -> {os.path.basename(path)}")
+
+
+def main():
+    gputools, imagetools, olaGPU = rh.load()
+    for name, spec in CASES.items():
+        make_case(name, *spec, gputools, imagetools, olaGPU)
+
+
+if __name__ == "__main__":
+    main()

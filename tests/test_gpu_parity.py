@@ -1,0 +1,283 @@
+"""GPU parity of the fused EFF kernels (through the C ABI) against the
+reference's golden vectors and the FP64 oracle.
+
+Tolerance: relative L2 <= 1e-5 (FP32 kernels vs FP64 oracle), the bound the
+operator's results are stated at.
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from oracle import eff64
+from vmbd_gb300 import geometry, synth
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-5
+GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "ref_*.npz")))
+
+
+def rel(a, b, mask=None):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    if mask is not None:
+        a, b = a[mask], b[mask]
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def t(a, dev):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a, np.float32)).to(dev)
+
+
+def make(sx, csf, sf, sw=None, hop=None, mode="valid", kind="gauss", seed=0):
+    wa = geometry.win2winaux(sx, csf, 0.5, sw=sw, nhop=hop)
+    g = eff64.Geometry(sx, sf, csf, wa.sw, wa.nhop, mode)
+    x = synth.blob_edge_image(sx, seed=seed)
+    gen = synth.gaussian_psfs if kind == "gauss" else synth.motion_psfs
+    f = gen(g.K, sf, seed=seed + 1)
+    r = np.random.default_rng(seed + 2).standard_normal(g.sy).astype(np.float32)
+    return wa, g, x, f, r
+
+
+# ---------------------------------------------------------------------------
+# golden vectors of the reference (OlaGPU run on its own kernels)
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("path", GOLDEN, ids=lambda p: os.path.basename(p))
+def test_olagpu_matches_reference_golden(cuda, path):
+    from vmbd_gb300 import OlaGPU
+    z = np.load(path)
+    c = {k: z[k] for k in z.files}
+    mode = str(c["mode"])
+    wa = geometry.Winaux(tuple(c["sx"]), tuple(c["csf"]), tuple(c["sw"]), tuple(c["hop"]))
+    F = OlaGPU(c["f"], tuple(c["sx"]), mode, wa, adjoint="reference")
+    X = OlaGPU(c["x"], tuple(c["sf"]), mode, wa, adjoint="reference")
+    y = F.cnv(c["x"])
+    yX = X.cnv(c["f"])
+    m = np.isfinite(c["y"])
+    assert rel(y, c["y"], m) < TOL
+    assert rel(yX, c["y"], m) < TOL
+    assert np.all(y[~m] == 0)
+    gx = F.cnvtp(c["r"])
+    gf = X.cnvtp(c["r"])
+    mx = np.isfinite(c["gx"])
+    assert rel(gx, c["gx"], mx) < TOL
+    assert rel(gf, c["gf"]) < TOL
+
+
+# ---------------------------------------------------------------------------
+# FP64 oracle, exact adjoints, at the workload geometries
+# ---------------------------------------------------------------------------
+CASES = {
+    # 256^2, 4x4 grid of 64^2 patches, 15^2 Gaussian PSFs, frame 128
+    "cfg1_literal": dict(sx=(256, 256), csf=(4, 4), sf=(15, 15), sw=(64, 64), hop=(32, 32)),
+    "cfg1_winaux": dict(sx=(256, 256), csf=(4, 4), sf=(15, 15)),
+    # 512^2, 8x8 grid of 96^2 patches, 31^2 motion PSFs, frame 128
+    "cfg2_literal": dict(sx=(512, 512), csf=(8, 8), sf=(31, 31), sw=(96, 96), hop=(48, 48), kind="motion"),
+    # 512^2, 8x8 winaux geometry (sw 122), frame 256
+    "cfg2_winaux": dict(sx=(512, 512), csf=(8, 8), sf=(31, 31), kind="motion"),
+    # 512^2 frame of the MFBD workload, 25^2 PSFs, sw 120, frame 256
+    "cfg3_winaux": dict(sx=(536, 536), csf=(8, 8), sf=(25, 25), kind="motion"),
+    # 384x512 member of the uneven batch: mixed-parity sw (116, 119)
+    "cfg4_mixed": dict(sx=(404, 532), csf=(6, 8), sf=(21, 21), kind="motion"),
+    "same_mode": dict(sx=(200, 232), csf=(3, 4), sf=(12, 10), mode="same"),
+    "full_mode": dict(sx=(200, 232), csf=(3, 4), sf=(12, 10), mode="full"),
+}
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_operator_matches_fp64_oracle(cuda, name):
+    from vmbd_gb300.eff import EffPlan
+    wa, g, x, f, r = make(**CASES[name])
+    plan = EffPlan(wa, g.sf, g.mode, device=cuda)
+    ws = wa.ws.astype(np.float64)
+    fh = plan.psf_spectrum(t(f, cuda))
+    xh_fwd = plan.empty_spectrum()
+    y = plan.forward_image(t(x, cuda), fh, xhat_out=xh_fwd).cpu().numpy()
+    y_ref = eff64.forward(x, f, g, ws)
+    assert rel(y, y_ref) < TOL, name
+    xh = plan.image_spectrum(t(x, cuda))
+    assert rel(plan.forward_psf(t(f, cuda), xh).cpu().numpy(), y_ref) < TOL
+    assert rel(xh_fwd.cpu().numpy(), xh.cpu().numpy()) < 1e-6
+    gx, gf = plan.adjoint(t(r, cuda), fh, xh)
+    assert rel(gx.cpu().numpy(), eff64.adjoint_image(r, f, g, ws)) < TOL
+    assert rel(gf.cpu().numpy(), eff64.adjoint_psf(r, x, g, ws)) < TOL
+    if g.mode != "full":
+        gx, gf = plan.adjoint(t(r, cuda), fh, xh, adjoint="reference")
+        assert rel(gx.cpu().numpy(), eff64.adjoint_image(r, f, g, ws, exact=False)) < TOL
+        assert rel(gf.cpu().numpy(), eff64.adjoint_psf(r, x, g, ws, exact=False)) < TOL
+
+
+def test_psf_spectrum_matches_numpy_fft(cuda):
+    from vmbd_gb300.eff import EffPlan
+    wa, g, x, f, r = make(**CASES["cfg2_literal"])
+    plan = EffPlan(wa, g.sf, device=cuda)
+    fh = plan.psf_spectrum(t(f, cuda)).cpu().numpy()  # [K, N/2+1, N]: column-major half spectrum
+    N = plan.N
+    ref = np.fft.rfft2(eff64.pad_stack(f, (N, N)))  # [K, N, N/2+1]
+    assert rel(fh, np.transpose(ref, (0, 2, 1))) < 1e-6
+
+
+def test_batched_launch_matches_single(cuda):
+    import torch
+    from vmbd_gb300.eff import EffPlan
+    wa, g, x, f, r = make(**CASES["cfg1_literal"])
+    plan = EffPlan(wa, g.sf, device=cuda)
+    B = 3
+    xs = np.stack([synth.blob_edge_image(g.sx, seed=s) for s in range(B)])
+    fs = np.stack([synth.gaussian_psfs(g.K, g.sf, seed=s + 9) for s in range(B)])
+    rs = np.random.default_rng(0).standard_normal((B,) + g.sy).astype(np.float32)
+    fh = plan.psf_spectrum(t(fs, cuda))
+    xh = plan.empty_spectrum(B)
+    y = plan.forward_image(t(xs, cuda), fh, xhat_out=xh)
+    gx, gf = plan.adjoint(t(rs, cuda), fh, xh)
+    for b in range(B):
+        fh1 = plan.psf_spectrum(t(fs[b], cuda))
+        xh1 = plan.image_spectrum(t(xs[b], cuda))
+        assert rel(y[b].cpu().numpy(), plan.forward_image(t(xs[b], cuda), fh1).cpu().numpy()) < 1e-6
+        gx1, gf1 = plan.adjoint(t(rs[b], cuda), fh1, xh1)
+        assert rel(gx[b].cpu().numpy(), gx1.cpu().numpy()) < 1e-6
+        assert rel(gf[b].cpu().numpy(), gf1.cpu().numpy()) < 1e-6
+    torch.cuda.synchronize()
+
+
+@pytest.mark.parametrize("name", ["cfg2_literal", "cfg2_winaux"])
+def test_adjoint_identity_on_gpu(cuda, name):
+    from vmbd_gb300.eff import EffPlan
+    wa, g, x, f, r = make(**CASES[name])
+    plan = EffPlan(wa, g.sf, device=cuda)
+    fh = plan.psf_spectrum(t(f, cuda))
+    xh = plan.image_spectrum(t(x, cuda))
+    y = plan.forward_image(t(x, cuda), fh).double().cpu().numpy()
+    gx, gf = plan.adjoint(t(r, cuda), fh, xh)
+    lhs = np.vdot(y, r)
+    assert abs(lhs - np.vdot(x, gx.double().cpu().numpy())) < 1e-5 * abs(lhs)
+    assert abs(lhs - np.vdot(f, gf.double().cpu().numpy())) < 1e-5 * abs(lhs)
+
+
+def test_delta_psf_identity_on_gpu(cuda):
+    from vmbd_gb300.eff import EffPlan
+    wa, g, x, f, r = make(**CASES["cfg2_literal"])
+    plan = EffPlan(wa, g.sf, device=cuda)
+    d = np.zeros_like(f)
+    d[:, 0, 0] = 1
+    y = plan.forward_image(t(x, cuda), plan.psf_spectrum(t(d, cuda))).cpu().numpy()
+    o = g.off
+    cov = tuple(min(g.sy[k], g.sxp[k] - o[k]) for k in range(2))  # region the grid covers
+    assert np.abs(y[:cov[0], :cov[1]] - x[o[0]:o[0] + cov[0], o[1]:o[1] + cov[1]]).max() < 1e-5
+    assert np.all(y[cov[0]:, :] == 0) and np.all(y[:, cov[1]:] == 0)
+
+
+def test_repeatable_psf_adjoint(cuda):
+    # the PSF adjoint uses no atomics: bitwise identical across runs
+    from vmbd_gb300.eff import EffPlan
+    wa, g, x, f, r = make(**CASES["cfg1_literal"])
+    plan = EffPlan(wa, g.sf, device=cuda)
+    xh = plan.image_spectrum(t(x, cuda))
+    a = plan.adjoint(t(r, cuda), xhat=xh, want_image=False)[1]
+    b = plan.adjoint(t(r, cuda), xhat=xh, want_image=False)[1]
+    assert bool((a == b).all())
+
+
+# ---------------------------------------------------------------------------
+# projections
+# ---------------------------------------------------------------------------
+def test_simplex_projection(cuda):
+    from vmbd_gb300.eff import project_psf
+    rng = np.random.default_rng(7)
+    f = rng.standard_normal((64, 25, 25)).astype(np.float32) * 0.05 + 1.0 / 625
+    f[3] = -1.0  # all negative
+    f[5] = 0.0
+    f[6, 3, 4] = 50.0  # one dominant entry
+    out = project_psf(t(f, cuda), "simplex").cpu().numpy()
+    ref = eff64.simplex_project(f)
+    assert np.abs(out - ref).max() < 2e-6
+    assert np.allclose(out.reshape(64, -1).sum(1), 1, atol=1e-5)
+
+
+def test_clip_normalize_projection(cuda):
+    from vmbd_gb300.eff import project_psf
+    rng = np.random.default_rng(8)
+    f = rng.standard_normal((16, 31, 31)).astype(np.float32)
+    f[2] = -abs(f[2])  # sums to 0 after clipping: left at 0
+    out = project_psf(t(f, cuda), "clip_normalize").cpu().numpy()
+    assert np.abs(out - eff64.clip_normalize(f)).max() < 1e-6
+
+
+def test_basis_project(cuda):
+    from vmbd_gb300.eff import basis_project
+    rng = np.random.default_rng(9)
+    fs = rng.standard_normal((25, 25)).astype(np.float32)
+    basis = rng.standard_normal((37, 25, 25)).astype(np.float32)
+    w = basis_project(t(fs, cuda), t(basis, cuda)).cpu().numpy()
+    assert rel(w, eff64.basis_project(fs, basis)) < 1e-5
+
+
+# ---------------------------------------------------------------------------
+# autograd
+# ---------------------------------------------------------------------------
+def test_autograd_gradients_and_finite_differences(cuda):
+    import torch
+    from vmbd_gb300.autograd import eff
+    from vmbd_gb300.eff import EffPlan
+    wa, g, x, f, r = make(**CASES["cfg2_literal"])
+    ws = wa.ws.astype(np.float64)
+    y_obs = (eff64.forward(x, f, g, ws) + 0.01 * np.random.default_rng(3).standard_normal(g.sy))
+    plan = EffPlan(wa, g.sf, device=cuda)
+    xt = t(x, cuda).requires_grad_()
+    ft = t(f, cuda).requires_grad_()
+    yt = t(y_obs, cuda)
+    loss = 0.5 * ((eff(xt, ft, plan) - yt) ** 2).sum()
+    loss.backward()
+    res = eff64.forward(x, f, g, ws) - y_obs
+    gx_ref = eff64.adjoint_image(res, f, g, ws)
+    gf_ref = eff64.adjoint_psf(res, x, g, ws)
+    assert rel(xt.grad.cpu().numpy(), gx_ref) < TOL
+    assert rel(ft.grad.cpu().numpy(), gf_ref) < TOL
+
+    # central finite differences (h = 1e-3) at 200 random coordinates of x and f,
+    # loss accumulated in FP64 from the FP32 forward
+    rng = np.random.default_rng(4)
+    h = 1e-3
+
+    def loss64(xv, fv):
+        with torch.no_grad():
+            yv = plan.forward_image(t(xv, cuda), plan.psf_spectrum(t(fv, cuda))).double().cpu().numpy()
+        return 0.5 * np.sum((yv - y_obs) ** 2)
+
+    fd, an = [], []
+    for _ in range(100):
+        i = tuple(rng.integers(0, s) for s in g.sx)
+        xp, xm = x.copy(), x.copy()
+        xp[i] += h
+        xm[i] -= h
+        fd.append((loss64(xp, f) - loss64(xm, f)) / (2 * h))
+        an.append(gx_ref[i])
+    for _ in range(100):
+        i = tuple(rng.integers(0, s) for s in (g.K,) + g.sf)
+        fp, fm = f.copy(), f.copy()
+        fp[i] += h
+        fm[i] -= h
+        fd.append((loss64(x, fp) - loss64(x, fm)) / (2 * h))
+        an.append(gf_ref[i])
+    # FP32 forward: each loss carries ~1e-7 relative rounding, divided by 2h
+    assert rel(np.array(fd), np.array(an)) < 2e-2
+
+
+def test_reference_error_behaviour(cuda):
+    from vmbd_gb300 import OlaGPU
+    wa = geometry.win2winaux((96, 96), (2, 2))
+    f = synth.gaussian_psfs(4, (9, 9))
+    with pytest.raises(IOError):
+        OlaGPU(synth.gaussian_psfs(3, (9, 9)), (96, 96), "valid", wa)
+    with pytest.raises(IOError):
+        OlaGPU(f, (90, 96), "valid", wa)
+    with pytest.raises(NotImplementedError):
+        OlaGPU(f, (96, 96), "circ", wa)
+    F = OlaGPU(f, (96, 96), "full", wa)
+    with pytest.raises(NotImplementedError):
+        F.cnvtp(np.zeros((104, 104), np.float32))
+    F = OlaGPU(f, (96, 96), "valid", wa)
+    with pytest.raises(IOError):
+        F.cnv(np.zeros((95, 96), np.float32))

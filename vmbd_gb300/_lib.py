@@ -1,0 +1,87 @@
+"""ctypes binding of ``libvmbd_eff.so`` (the C ABI in include/vmbd_eff.h).
+
+The library is built in tree by ``vmbd_gb300.build``.  Loading fails loudly:
+there is no CPU fallback for any operation of this package.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+from . import build as _build
+
+EFF_OK = 0
+EFF_ERR_INVALID = 1
+EFF_ERR_UNSUPPORTED = 2
+EFF_ERR_CUDA = 3
+
+MODES = {"valid": 0, "same": 1, "full": 2}
+ADJ_EXACT = 0
+ADJ_REFERENCE = 1
+PROJ_CLIP_NORMALIZE = 0
+PROJ_SIMPLEX = 1
+
+# Every symbol include/vmbd_eff.h declares.
+EXPORTS = (
+    "eff_plan_create", "eff_plan_destroy", "eff_plan_frame", "eff_spectrum_bytes",
+    "eff_psf_spectrum", "eff_image_spectrum", "eff_forward_image", "eff_forward_psf",
+    "eff_adjoint", "eff_project_psf", "eff_basis_project", "eff_last_error",
+)
+
+
+class EffGeom(ctypes.Structure):
+    _fields_ = [("sx", ctypes.c_int * 2), ("sf", ctypes.c_int * 2), ("csf", ctypes.c_int * 2),
+                ("sw", ctypes.c_int * 2), ("hop", ctypes.c_int * 2), ("sfft", ctypes.c_int),
+                ("mode", ctypes.c_int)]
+
+
+class EffError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"vmbd_eff error {code}: {msg}")
+        self.code = code
+
+
+_LIB = None
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True) -> ctypes.CDLL:
+    """Load the library (building it first when it is missing or stale)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if build_if_missing and not _build.up_to_date():
+        _build.build()
+    if not os.path.exists(_build.LIB):
+        raise RuntimeError(f"{_build.LIB} is missing: run vmbd_gb300.build.build()")
+    L = ctypes.CDLL(_build.LIB)
+    vp, ip, fp = ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p
+    sig = {
+        "eff_plan_create": ([ctypes.POINTER(EffGeom), fp, fp, ctypes.POINTER(vp)], ip),
+        "eff_plan_destroy": ([vp], ip),
+        "eff_plan_frame": ([vp, ctypes.POINTER(ctypes.c_int)], ip),
+        "eff_spectrum_bytes": ([vp], ctypes.c_size_t),
+        "eff_psf_spectrum": ([vp, fp, vp, ip, vp], ip),
+        "eff_image_spectrum": ([vp, fp, vp, ip, vp], ip),
+        "eff_forward_image": ([vp, fp, vp, fp, vp, ip, vp], ip),
+        "eff_forward_psf": ([vp, fp, vp, fp, vp, ip, vp], ip),
+        "eff_adjoint": ([vp, fp, vp, vp, fp, fp, ip, ip, vp], ip),
+        "eff_project_psf": ([fp, ip, ip, ip, vp], ip),
+        "eff_basis_project": ([fp, fp, fp, ip, ip, vp], ip),
+        "eff_last_error": ([], ctypes.c_char_p),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = res
+    _LIB = L
+    return L
+
+
+def check(status: int) -> None:
+    if status != EFF_OK:
+        msg = load().eff_last_error().decode(errors="replace")
+        raise EffError(status, msg)

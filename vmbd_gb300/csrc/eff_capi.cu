@@ -1,0 +1,311 @@
+// C ABI of the EFF operator (declared in include/vmbd_eff.h).
+//
+// Plan creation validates the geometry as OlaGPU.__init__ does
+// (olaGPU.py:95-168), uploads the separable window factors and the FP64-built
+// twiddle table, and picks the FFT frame.  The compute entry points only
+// enqueue work on the caller's stream (memset of atomically accumulated
+// outputs + one kernel) and allocate nothing.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "eff_launch.cuh"
+#include "../../include/vmbd_eff.h"
+
+namespace eff {
+cudaError_t launch_project(float* f, int K, int n, int mode, cudaStream_t st);
+cudaError_t launch_basis_project(const float* fs, const float* basis, float* w, int nb, int n,
+                                 cudaStream_t st);
+}  // namespace eff
+
+struct EffPlan {
+  EffGeom g;
+  int N;
+  int K;
+  int sy[2], off[2], E[2];
+  int threads;
+  int device;
+  float2* win0;
+  float2* win1;
+  float2* tw;
+};
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+  return fail(EFF_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+int frame_ok(int n) { return n == 64 || n == 128 || n == 256; }
+
+eff::Params base_params(const EffPlan* p) {
+  eff::Params P;
+  std::memset(&P, 0, sizeof(P));
+  const EffGeom& g = p->g;
+  P.sx0 = g.sx[0]; P.sx1 = g.sx[1];
+  P.sf0 = g.sf[0]; P.sf1 = g.sf[1];
+  P.csf0 = g.csf[0]; P.csf1 = g.csf[1];
+  P.sw0 = g.sw[0]; P.sw1 = g.sw[1];
+  P.hop0 = g.hop[0]; P.hop1 = g.hop[1];
+  P.sy0 = p->sy[0]; P.sy1 = p->sy[1];
+  P.off0 = p->off[0]; P.off1 = p->off[1];
+  P.E0 = p->E[0]; P.E1 = p->E[1];
+  P.lo0 = 0; P.hi0 = p->E[0]; P.lo1 = 0; P.hi1 = p->E[1];
+  P.win0 = p->win0;
+  P.win1 = p->win1;
+  P.tw = p->tw;
+  P.x_bs = (long long)g.sx[0] * g.sx[1];
+  P.f_bs = (long long)p->K * g.sf[0] * g.sf[1];
+  P.y_bs = (long long)p->sy[0] * p->sy[1];
+  P.spec_bs = (long long)p->K * (p->N / 2 + 1) * p->N;
+  return P;
+}
+
+int run(const EffPlan* p, int op, const eff::Params& P, int batch, void* stream) {
+  const size_t smem = eff::smem_bytes(p->N, op, P, p->threads);
+  if (smem > 227u * 1024u)
+    return fail(EFF_ERR_UNSUPPORTED, "frame needs " + std::to_string(smem) + " bytes of shared memory");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  cudaError_t e;
+  switch (p->N) {
+    case 64: e = eff::launch_n64(op, P, p->K, batch, p->threads, smem, st); break;
+    case 128: e = eff::launch_n128(op, P, p->K, batch, p->threads, smem, st); break;
+    case 256: e = eff::launch_n256(op, P, p->K, batch, p->threads, smem, st); break;
+    default: return fail(EFF_ERR_UNSUPPORTED, "frame size");
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
+  return EFF_OK;
+}
+
+int check_plan(const EffPlan* p, int batch) {
+  if (!p) return fail(EFF_ERR_INVALID, "null plan");
+  if (batch < 1 || batch > 65535) return fail(EFF_ERR_INVALID, "batch must be in [1, 65535]");
+  return EFF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* eff_last_error(void) { return g_last_error.c_str(); }
+
+int eff_plan_create(const EffGeom* geom, const float* win0, const float* win1, EffPlan** plan) {
+  if (!geom || !win0 || !win1 || !plan) return fail(EFF_ERR_INVALID, "null argument");
+  *plan = nullptr;
+  const EffGeom& g = *geom;
+  for (int d = 0; d < 2; ++d) {
+    if (g.sx[d] < 1 || g.sf[d] < 1 || g.csf[d] < 1 || g.sw[d] < 1 || g.hop[d] < 1)
+      return fail(EFF_ERR_INVALID, "sizes must be positive");
+    if (g.sf[d] >= g.sx[d])
+      return fail(EFF_ERR_INVALID, "Size missmatch: PSF must be smaller than the image");
+  }
+  if (g.mode < EFF_MODE_VALID || g.mode > EFF_MODE_FULL) return fail(EFF_ERR_INVALID, "Not a valid mode!");
+  if ((long long)g.csf[0] * g.csf[1] > 65535) return fail(EFF_ERR_UNSUPPORTED, "too many patches");
+
+  EffPlan p;
+  std::memset(&p, 0, sizeof(p));
+  p.g = g;
+  p.K = g.csf[0] * g.csf[1];
+  for (int d = 0; d < 2; ++d) {
+    p.E[d] = g.sw[d] + g.sf[d] - 1;
+    if (g.mode == EFF_MODE_VALID) { p.sy[d] = g.sx[d] - g.sf[d] + 1; p.off[d] = g.sf[d] - 1; }
+    else if (g.mode == EFF_MODE_SAME) { p.sy[d] = g.sx[d]; p.off[d] = g.sf[d] / 2; }
+    else { p.sy[d] = g.sx[d] + g.sf[d] - 1; p.off[d] = 0; }
+  }
+  const int emax = p.E[0] > p.E[1] ? p.E[0] : p.E[1];
+  if (g.sfft == 0) {
+    int n = 64;
+    while (n < emax) n <<= 1;
+    p.N = n;
+  } else {
+    p.N = g.sfft;
+  }
+  if (!frame_ok(p.N))
+    return fail(EFF_ERR_UNSUPPORTED, "FFT frame " + std::to_string(p.N) +
+                                         " (needs a power of two in [64, 256] >= sw + sf - 1 = " +
+                                         std::to_string(emax) + ")");
+  if (p.N < emax) return fail(EFF_ERR_INVALID, "FFT frame smaller than sw + sf - 1");
+
+  // Threads per CTA: 256, or 128 when the frame plus exchange scratch would
+  // not fit in shared memory otherwise.
+  p.threads = 256;
+  {
+    eff::Params P = base_params(&p);
+    P.out0 = reinterpret_cast<float*>(1);
+    P.out1 = reinterpret_cast<float*>(1);
+    size_t worst = 0;
+    for (int op = 0; op <= 4; ++op) {
+      const size_t s = eff::smem_bytes(p.N, op, P, 256);
+      if (s > worst) worst = s;
+    }
+    if (worst > 227u * 1024u) p.threads = 128;
+  }
+
+  cudaError_t e = cudaGetDevice(&p.device);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+
+  // Twiddle table [k1*G + g] = exp(-2 pi i g k1 / N), FP64 then rounded.
+  const int G = p.N / 16;
+  std::vector<float2> tw(p.N);
+  for (int k1 = 0; k1 < 16; ++k1)
+    for (int gg = 0; gg < G; ++gg) {
+      const double a = -2.0 * M_PI * double(gg * k1) / double(p.N);
+      tw[k1 * G + gg] = make_float2((float)std::cos(a), (float)std::sin(a));
+    }
+  const size_t n0 = 2 * (size_t)g.csf[0] * g.sw[0], n1 = 2 * (size_t)g.csf[1] * g.sw[1];
+  if ((e = cudaMalloc(&p.tw, sizeof(float2) * p.N)) != cudaSuccess) return cuda_fail(e, "cudaMalloc");
+  if ((e = cudaMalloc(&p.win0, sizeof(float) * n0)) != cudaSuccess) {
+    cudaFree(p.tw);
+    return cuda_fail(e, "cudaMalloc");
+  }
+  if ((e = cudaMalloc(&p.win1, sizeof(float) * n1)) != cudaSuccess) {
+    cudaFree(p.tw);
+    cudaFree(p.win0);
+    return cuda_fail(e, "cudaMalloc");
+  }
+  if ((e = cudaMemcpy(p.tw, tw.data(), sizeof(float2) * p.N, cudaMemcpyHostToDevice)) != cudaSuccess ||
+      (e = cudaMemcpy(p.win0, win0, sizeof(float) * n0, cudaMemcpyHostToDevice)) != cudaSuccess ||
+      (e = cudaMemcpy(p.win1, win1, sizeof(float) * n1, cudaMemcpyHostToDevice)) != cudaSuccess) {
+    cudaFree(p.tw);
+    cudaFree(p.win0);
+    cudaFree(p.win1);
+    return cuda_fail(e, "cudaMemcpy");
+  }
+  EffPlan* out = new (std::nothrow) EffPlan(p);
+  if (!out) {
+    cudaFree(p.tw);
+    cudaFree(p.win0);
+    cudaFree(p.win1);
+    return fail(EFF_ERR_INVALID, "out of host memory");
+  }
+  *plan = out;
+  return EFF_OK;
+}
+
+int eff_plan_destroy(EffPlan* plan) {
+  if (!plan) return EFF_OK;
+  cudaFree(plan->tw);
+  cudaFree(plan->win0);
+  cudaFree(plan->win1);
+  delete plan;
+  return EFF_OK;
+}
+
+int eff_plan_frame(const EffPlan* plan, int* n) {
+  if (!plan || !n) return fail(EFF_ERR_INVALID, "null argument");
+  *n = plan->N;
+  return EFF_OK;
+}
+
+size_t eff_spectrum_bytes(const EffPlan* plan) {
+  if (!plan) return 0;
+  return sizeof(float2) * (size_t)plan->K * (plan->N / 2 + 1) * plan->N;
+}
+
+int eff_psf_spectrum(const EffPlan* plan, const float* f, void* fhat, int batch, void* stream) {
+  if (int s = check_plan(plan, batch)) return s;
+  if (!f || !fhat) return fail(EFF_ERR_INVALID, "null argument");
+  eff::Params P = base_params(plan);
+  P.f = f;
+  P.a_out = static_cast<float2*>(fhat);
+  return run(plan, eff::OP_SPEC_PSF, P, batch, stream);
+}
+
+int eff_image_spectrum(const EffPlan* plan, const float* x, void* xhat, int batch, void* stream) {
+  if (int s = check_plan(plan, batch)) return s;
+  if (!x || !xhat) return fail(EFF_ERR_INVALID, "null argument");
+  eff::Params P = base_params(plan);
+  P.x = x;
+  P.a_out = static_cast<float2*>(xhat);
+  return run(plan, eff::OP_SPEC_IMAGE, P, batch, stream);
+}
+
+int eff_forward_image(const EffPlan* plan, const float* x, const void* fhat, float* y,
+                      void* xhat_out, int batch, void* stream) {
+  if (int s = check_plan(plan, batch)) return s;
+  if (!x || !fhat || !y) return fail(EFF_ERR_INVALID, "null argument");
+  eff::Params P = base_params(plan);
+  P.x = x;
+  P.b0 = static_cast<const float2*>(fhat);
+  P.out0 = y;
+  P.out0_bs = P.y_bs;
+  P.a_out = static_cast<float2*>(xhat_out);
+  cudaError_t e = cudaMemsetAsync(y, 0, sizeof(float) * P.y_bs * batch, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+  return run(plan, eff::OP_FWD_IMAGE, P, batch, stream);
+}
+
+int eff_forward_psf(const EffPlan* plan, const float* f, const void* xhat, float* y,
+                    void* fhat_out, int batch, void* stream) {
+  if (int s = check_plan(plan, batch)) return s;
+  if (!f || !xhat || !y) return fail(EFF_ERR_INVALID, "null argument");
+  eff::Params P = base_params(plan);
+  P.f = f;
+  P.b0 = static_cast<const float2*>(xhat);
+  P.out0 = y;
+  P.out0_bs = P.y_bs;
+  P.a_out = static_cast<float2*>(fhat_out);
+  cudaError_t e = cudaMemsetAsync(y, 0, sizeof(float) * P.y_bs * batch, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+  return run(plan, eff::OP_FWD_PSF, P, batch, stream);
+}
+
+int eff_adjoint(const EffPlan* plan, const float* y, const void* fhat, const void* xhat, float* gx,
+                float* gf, int adj_mode, int batch, void* stream) {
+  if (int s = check_plan(plan, batch)) return s;
+  if (!y || (!gx && !gf)) return fail(EFF_ERR_INVALID, "null argument");
+  if (gx && !fhat) return fail(EFF_ERR_INVALID, "image adjoint needs the PSF spectrum");
+  if (gf && !xhat) return fail(EFF_ERR_INVALID, "PSF adjoint needs the image spectrum");
+  if (adj_mode != EFF_ADJ_EXACT && adj_mode != EFF_ADJ_REFERENCE)
+    return fail(EFF_ERR_INVALID, "adj_mode");
+  if (adj_mode == EFF_ADJ_REFERENCE && plan->g.mode == EFF_MODE_FULL)
+    return fail(EFF_ERR_INVALID, "Not a valid mode!");  // olaGPU.py:285-286
+  eff::Params P = base_params(plan);
+  P.y = y;
+  P.b0 = static_cast<const float2*>(fhat);
+  P.b1 = static_cast<const float2*>(xhat);
+  P.out0 = gx;
+  P.out1 = gf;
+  P.out0_bs = P.x_bs;
+  P.out1_bs = P.f_bs;
+  if (adj_mode == EFF_ADJ_REFERENCE) {
+    // chop_pad_GPU at offset `off`, extent sw (olaGPU.py:276-286).
+    P.lo0 = plan->off[0];
+    P.hi0 = plan->off[0] + plan->g.sw[0] < plan->E[0] ? plan->off[0] + plan->g.sw[0] : plan->E[0];
+    P.lo1 = plan->off[1];
+    P.hi1 = plan->off[1] + plan->g.sw[1] < plan->E[1] ? plan->off[1] + plan->g.sw[1] : plan->E[1];
+  }
+  if (gx) {
+    cudaError_t e = cudaMemsetAsync(gx, 0, sizeof(float) * P.x_bs * batch, static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+  }
+  return run(plan, eff::OP_ADJ, P, batch, stream);
+}
+
+int eff_project_psf(float* f, int K, int n, int proj_mode, void* stream) {
+  if (!f || K < 1 || n < 1) return fail(EFF_ERR_INVALID, "bad argument");
+  if (proj_mode != EFF_PROJ_CLIP_NORMALIZE && proj_mode != EFF_PROJ_SIMPLEX)
+    return fail(EFF_ERR_INVALID, "proj_mode");
+  cudaError_t e = eff::launch_project(f, K, n, proj_mode, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "projection launch");
+  return EFF_OK;
+}
+
+int eff_basis_project(const float* fs, const float* basis, float* w, int nb, int n, void* stream) {
+  if (!fs || !basis || !w || nb < 1 || n < 1) return fail(EFF_ERR_INVALID, "bad argument");
+  cudaError_t e = eff::launch_basis_project(fs, basis, w, nb, n, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "basis projection launch");
+  return EFF_OK;
+}
+
+}  // extern "C"

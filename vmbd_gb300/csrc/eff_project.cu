@@ -1,0 +1,111 @@
+// PSF projections (one CTA per PSF) and the basis dot product.
+//
+// clip_normalize: the reference's PSF constraint -- non-negativity (L-BFGS-B
+//   bounds, olaGPU.py:404-411; cliplower_GPU, gputools.py:478-486) then
+//   per-PSF unit sum when the sum exceeds 1e-6 (normalize,
+//   gputools.py:1025-1044, which the reference runs on the host).
+// simplex: Euclidean projection onto {f >= 0, sum f = 1} by Michelot's
+//   active-set iteration (Michelot 1986): tau = (sum_{f_i > tau} f_i - 1) /
+//   #{f_i > tau}, repeated until the active set stops shrinking (at most n
+//   rounds; tau never decreases), then f = max(f - tau, 0).  Same result as
+//   the sort-based method of Duchi et al. 2008.
+// basis_project: w[b] = <fs, basis_b>, what projection.cu:3-27 computes for a
+//   correct block/column indexing.
+// All reductions are fixed-order trees, so results are run-to-run identical.
+#include <cuda_runtime.h>
+
+namespace eff {
+
+constexpr int kProjThreads = 256;
+
+// Deterministic block sum of (a, b); every thread gets the totals.
+__device__ __forceinline__ float2 block_sum2(float a, float b, float2* red) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, o);
+    b += __shfl_xor_sync(0xffffffffu, b, o);
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) red[w] = make_float2(a, b);
+  __syncthreads();
+  const int nw = blockDim.x >> 5;
+  float2 t = l < nw ? red[l] : make_float2(0.f, 0.f);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    t.x += __shfl_xor_sync(0xffffffffu, t.x, o);
+    t.y += __shfl_xor_sync(0xffffffffu, t.y, o);
+  }
+  return t;
+}
+
+__global__ void __launch_bounds__(kProjThreads) clip_normalize_kernel(float* f, int n) {
+  __shared__ float2 red[32];
+  float* p = f + (long long)blockIdx.x * n;
+  float s = 0.f;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const float v = fmaxf(p[i], 0.f);
+    p[i] = v;
+    s += v;
+  }
+  const float tot = block_sum2(s, 0.f, red).x;
+  if (tot > 1e-6f) {
+    const float inv = 1.f / tot;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) p[i] = p[i] * inv;
+  }
+}
+
+__global__ void __launch_bounds__(kProjThreads) simplex_kernel(float* f, int n) {
+  __shared__ float2 red[32];
+  float* p = f + (long long)blockIdx.x * n;
+  float s = 0.f;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s += p[i];
+  float2 t = block_sum2(s, 0.f, red);
+  float tau = (t.x - 1.f) / float(n);
+  int count = n;
+  for (int it = 0; it <= n; ++it) {
+    float ss = 0.f, cc = 0.f;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      const float v = p[i];
+      if (v > tau) {
+        ss += v;
+        cc += 1.f;
+      }
+    }
+    t = block_sum2(ss, cc, red);
+    const int c = int(t.y + 0.5f);
+    if (c == 0) break;
+    const float tn = (t.x - 1.f) / t.y;
+    if (c == count) {
+      tau = tn;
+      break;
+    }
+    count = c;
+    tau = tn;
+  }
+  for (int i = threadIdx.x; i < n; i += blockDim.x) p[i] = fmaxf(p[i] - tau, 0.f);
+}
+
+__global__ void __launch_bounds__(kProjThreads) basis_project_kernel(const float* fs, const float* basis,
+                                                                     float* w, int n) {
+  __shared__ float2 red[32];
+  const float* bp = basis + (long long)blockIdx.x * n;
+  float s = 0.f;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s = fmaf(__ldg(fs + i), __ldg(bp + i), s);
+  const float tot = block_sum2(s, 0.f, red).x;
+  if (threadIdx.x == 0) w[blockIdx.x] = tot;
+}
+
+cudaError_t launch_project(float* f, int K, int n, int mode, cudaStream_t st) {
+  if (mode == 0) clip_normalize_kernel<<<K, kProjThreads, 0, st>>>(f, n);
+  else simplex_kernel<<<K, kProjThreads, 0, st>>>(f, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_basis_project(const float* fs, const float* basis, float* w, int nb, int n,
+                                 cudaStream_t st) {
+  basis_project_kernel<<<nb, kProjThreads, 0, st>>>(fs, basis, w, n);
+  return cudaGetLastError();
+}
+
+}  // namespace eff

@@ -1,0 +1,211 @@
+"""Torch-level EFF operator: one plan per geometry, CUDA kernels via the C ABI.
+
+``EffPlan`` wraps ``eff_plan_create`` for a ``Winaux`` + PSF size + mode and
+exposes the kernels on torch CUDA tensors (float32, C order; an optional
+leading batch dim runs several images of the same geometry in one launch).
+Outputs and spectrum caches are allocated by torch; every kernel runs on the
+current torch stream.  Spectra are complex64 tensors of shape
+``[batch?, K, N/2+1, N]``.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from .geometry import Winaux
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def _stream(device):
+    return ctypes.c_void_p(torch.cuda.current_stream(device).cuda_stream)
+
+
+class EffPlan:
+    """Plan for ``y = EFF(x, f)`` on one geometry (OlaGPU.__init__,
+    olaGPU.py:95-168, without the cached spectrum)."""
+
+    def __init__(self, winaux: Winaux, sf, mode: str = "valid", sfft: int = 0, device=None):
+        if mode not in _lib.MODES:
+            raise NotImplementedError("Not a valid mode!")
+        self.lib = _lib.load()
+        self.winaux = winaux
+        self.sf = (int(sf[0]), int(sf[1]))
+        self.sx = winaux.sx
+        self.mode = mode
+        self.device = torch.device(device if device is not None else "cuda", )
+        if self.device.index is None:
+            self.device = torch.device("cuda", torch.cuda.current_device())
+        g = _lib.EffGeom()
+        g.sx[:] = self.sx
+        g.sf[:] = self.sf
+        g.csf[:] = winaux.csf
+        g.sw[:] = winaux.sw
+        g.hop[:] = winaux.nhop
+        g.sfft = int(sfft)
+        g.mode = _lib.MODES[mode]
+        self._w0 = np.ascontiguousarray(winaux.win0, dtype=np.float32)
+        self._w1 = np.ascontiguousarray(winaux.win1, dtype=np.float32)
+        h = ctypes.c_void_p()
+        with torch.cuda.device(self.device):
+            _lib.check(self.lib.eff_plan_create(ctypes.byref(g), self._w0.ctypes.data,
+                                                self._w1.ctypes.data, ctypes.byref(h)))
+        self._h = h
+        n = ctypes.c_int()
+        _lib.check(self.lib.eff_plan_frame(h, ctypes.byref(n)))
+        self.N = n.value
+        self.K = winaux.K
+        off = {"valid": [v - 1 for v in self.sf], "same": [v // 2 for v in self.sf], "full": [0, 0]}
+        self.off = tuple(off[mode])
+        if mode == "valid":
+            self.sy = tuple(self.sx[d] - self.sf[d] + 1 for d in range(2))
+        elif mode == "same":
+            self.sy = self.sx
+        else:
+            self.sy = tuple(self.sx[d] + self.sf[d] - 1 for d in range(2))
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                self.lib.eff_plan_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    # ------------------------------------------------------------------
+    @property
+    def spectrum_shape(self) -> tuple:
+        return (self.K, self.N // 2 + 1, self.N)
+
+    def empty_spectrum(self, batch=None) -> torch.Tensor:
+        shape = ((batch,) if batch else ()) + self.spectrum_shape
+        return torch.empty(shape, dtype=torch.complex64, device=self.device)
+
+    def _check(self, t, shape, name):
+        if not isinstance(t, torch.Tensor) or not t.is_cuda:
+            raise TypeError(f"{name} must be a CUDA tensor")
+        if t.dtype != torch.float32:
+            raise TypeError(f"{name} must be float32")
+        if tuple(t.shape[-len(shape):]) != tuple(shape):
+            raise IOError(f"Size missmatch: {name} has shape {tuple(t.shape)}, expected "
+                          f"[..., {', '.join(map(str, shape))}]")
+        extra = t.dim() - len(shape)
+        if extra > 1:
+            raise IOError(f"{name}: at most one batch dimension")
+        if t.device != self.device:
+            raise ValueError(f"{name} is on {t.device}, plan on {self.device}")
+        return t.contiguous(), (t.shape[0] if extra == 1 else None)
+
+    def _check_spec(self, s, batch, name):
+        shape = ((batch,) if batch else ()) + self.spectrum_shape
+        if s.dtype != torch.complex64 or tuple(s.shape) != shape or not s.is_contiguous():
+            raise IOError(f"{name} must be a contiguous complex64 tensor of shape {shape}")
+        return s
+
+    # ------------------------------------------------------------------
+    def psf_spectrum(self, f, out=None):
+        f, b = self._check(f, (self.K,) + self.sf, "f")
+        out = self.empty_spectrum(b) if out is None else self._check_spec(out, b, "out")
+        _lib.check(self.lib.eff_psf_spectrum(self._h, _ptr(f), _ptr(out), b or 1, _stream(self.device)))
+        return out
+
+    def image_spectrum(self, x, out=None):
+        x, b = self._check(x, self.sx, "x")
+        out = self.empty_spectrum(b) if out is None else self._check_spec(out, b, "out")
+        _lib.check(self.lib.eff_image_spectrum(self._h, _ptr(x), _ptr(out), b or 1, _stream(self.device)))
+        return out
+
+    def forward_image(self, x, fhat, out=None, xhat_out=None):
+        """F.cnv(x): y = EFF(x, f) with f given by its spectrum."""
+        x, b = self._check(x, self.sx, "x")
+        self._check_spec(fhat, b, "fhat")
+        if xhat_out is not None:
+            self._check_spec(xhat_out, b, "xhat_out")
+        if out is None:
+            out = torch.empty(((b,) if b else ()) + self.sy, dtype=torch.float32, device=self.device)
+        _lib.check(self.lib.eff_forward_image(self._h, _ptr(x), _ptr(fhat), _ptr(out), _ptr(xhat_out),
+                                              b or 1, _stream(self.device)))
+        return out
+
+    def forward_psf(self, f, xhat, out=None, fhat_out=None):
+        """X.cnv(f): y = EFF(x, f) with x given by its windowed-patch spectrum."""
+        f, b = self._check(f, (self.K,) + self.sf, "f")
+        self._check_spec(xhat, b, "xhat")
+        if fhat_out is not None:
+            self._check_spec(fhat_out, b, "fhat_out")
+        if out is None:
+            out = torch.empty(((b,) if b else ()) + self.sy, dtype=torch.float32, device=self.device)
+        _lib.check(self.lib.eff_forward_psf(self._h, _ptr(f), _ptr(xhat), _ptr(out), _ptr(fhat_out),
+                                            b or 1, _stream(self.device)))
+        return out
+
+    def adjoint(self, y, fhat=None, xhat=None, want_image=True, want_psf=True,
+                adjoint="exact", gx=None, gf=None):
+        """F.cnvtp(y) and/or X.cnvtp(y) from one transform of y.
+
+        Returns ``(gx, gf)``; an output that is not wanted is None.
+        ``adjoint``: 'exact' (transpose of the forward) or 'reference'
+        (OlaGPU.cnvtp's truncated chop)."""
+        if adjoint not in ("exact", "reference"):
+            raise ValueError("adjoint must be 'exact' or 'reference'")
+        if adjoint == "reference" and self.mode not in ("valid", "same"):
+            raise NotImplementedError("Not a valid mode!")
+        y, b = self._check(y, self.sy, "y")
+        want_image = want_image and fhat is not None
+        want_psf = want_psf and xhat is not None
+        if not (want_image or want_psf):
+            raise ValueError("adjoint needs fhat (image gradient) and/or xhat (PSF gradient)")
+        lead = (b,) if b else ()
+        if want_image:
+            self._check_spec(fhat, b, "fhat")
+            if gx is None:
+                gx = torch.empty(lead + self.sx, dtype=torch.float32, device=self.device)
+        else:
+            gx = None
+        if want_psf:
+            self._check_spec(xhat, b, "xhat")
+            if gf is None:
+                gf = torch.empty(lead + (self.K,) + self.sf, dtype=torch.float32, device=self.device)
+        else:
+            gf = None
+        mode = _lib.ADJ_EXACT if adjoint == "exact" else _lib.ADJ_REFERENCE
+        _lib.check(self.lib.eff_adjoint(self._h, _ptr(y), _ptr(fhat if want_image else None),
+                                        _ptr(xhat if want_psf else None), _ptr(gx), _ptr(gf), mode,
+                                        b or 1, _stream(self.device)))
+        return gx, gf
+
+
+def project_psf(f: torch.Tensor, mode: str = "simplex") -> torch.Tensor:
+    """In-place PSF projection of a [..., K, sf0, sf1] stack: 'simplex'
+    (Euclidean projection onto the unit simplex) or 'clip_normalize' (the
+    reference's non-negativity + normalize, gputools.py:1025-1044)."""
+    if not f.is_cuda or f.dtype != torch.float32 or not f.is_contiguous():
+        raise TypeError("f must be a contiguous float32 CUDA tensor")
+    lib = _lib.load()
+    m = {"simplex": _lib.PROJ_SIMPLEX, "clip_normalize": _lib.PROJ_CLIP_NORMALIZE}[mode]
+    n = f.shape[-1] * f.shape[-2]
+    K = f.numel() // n
+    with torch.cuda.device(f.device):
+        _lib.check(lib.eff_project_psf(_ptr(f), K, n, m, _stream(f.device)))
+    return f
+
+
+def basis_project(fs: torch.Tensor, basis: torch.Tensor) -> torch.Tensor:
+    """``w[b] = <fs, basis[b]>`` (projection.cu:3-27 as intended)."""
+    lib = _lib.load()
+    fs = fs.contiguous()
+    basis = basis.contiguous()
+    n = fs.numel()
+    nb = basis.shape[0]
+    if basis.numel() != nb * n:
+        raise IOError("Size missmatch between basis and fs")
+    w = torch.empty(nb, dtype=torch.float32, device=fs.device)
+    with torch.cuda.device(fs.device):
+        _lib.check(lib.eff_basis_project(_ptr(fs), _ptr(basis), _ptr(w), nb, n, _stream(fs.device)))
+    return w

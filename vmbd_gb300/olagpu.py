@@ -1,0 +1,99 @@
+"""Drop-in ``OlaGPU`` (olaGPU.py:11-311): same constructor, ``cnv`` and
+``cnvtp``, backed by the fused sm_103a kernels.
+
+``OlaGPU(z, sx, mode, winaux)``: a 3-D ``z`` (PSF stack) with ``sx`` larger
+than the PSFs makes an F object that caches the PSF spectrum; a 2-D ``z``
+(image) with ``sx`` smaller than it (``sx`` is then the PSF size) makes an X
+object that caches the windowed-patch spectrum (olaGPU.py:104-121).
+``cnv(u)`` applies the operator to an image (F) or a PSF stack (X);
+``cnvtp(y)`` applies its transpose.  Inputs may be numpy arrays (returned
+as numpy, host copies included, olaGPU.py:254-257) or float32 CUDA tensors
+(returned as tensors).  Errors follow the reference: ``IOError`` on a size
+mismatch, ``NotImplementedError`` on an unsupported mode.
+
+One addition: ``adjoint='exact'`` (default) makes ``cnvtp`` the exact
+transpose of ``cnv``; ``adjoint='reference'`` reproduces the reference's
+``cnvtp``, whose chop of ``y`` drops the first ``sf-1`` rows/columns of each
+patch's support (olaGPU.py:276-286).
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from .eff import EffPlan
+from .geometry import Winaux
+
+
+def _to_device(a, device):
+    if isinstance(a, torch.Tensor):
+        if not a.is_cuda:
+            a = a.to(device)
+        return a.to(torch.float32).contiguous(), False
+    t = torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32))
+    return t.pin_memory().to(device, non_blocking=True), True
+
+
+class OlaGPU:
+    def __init__(self, f, sx, mode, winaux: Winaux, adjoint: str = "exact", sfft: int = 0):
+        sf = np.array(f.shape)[-2:]
+        sx = np.array(sx)
+        csf = winaux.csf
+        if len(f.shape) == 3 and np.all(sx > sf):
+            self.__id__ = "F"
+            if f.shape[0] != csf[0] * csf[1]:
+                raise IOError("Size missmatch between winaux and PSF size!")
+        elif len(f.shape) == 2 and np.all(sx < sf):
+            self.__id__ = "X"
+            sf = sx
+            sx = np.array(f.shape)
+        else:
+            raise IOError("Size missmatch")
+        if tuple(int(v) for v in winaux.sx) != tuple(int(v) for v in sx):
+            raise IOError("Size missmatch between winaux and image size!")
+        if mode not in ("valid", "same", "full"):
+            raise NotImplementedError("Not a valid mode!")
+        if adjoint not in ("exact", "reference"):
+            raise ValueError("adjoint must be 'exact' or 'reference'")
+        self.device = f.device if isinstance(f, torch.Tensor) and f.is_cuda else \
+            torch.device("cuda", torch.cuda.current_device())
+        self.plan = EffPlan(winaux, tuple(int(v) for v in sf), mode, sfft=sfft, device=self.device)
+        self.winaux = winaux
+        self.mode = mode
+        self.adjoint = adjoint
+        self.sf = tuple(int(v) for v in sf)
+        self.sx = tuple(int(v) for v in sx)
+        self.sy = self.plan.sy
+        z, _ = _to_device(f, self.device)
+        if self.__id__ == "F":
+            self.f, self.x = z, None
+            self.fft_gpu = self.plan.psf_spectrum(z)
+        else:
+            self.f, self.x = None, z
+            self.fft_gpu = self.plan.image_spectrum(z)
+
+    def cnv(self, u):
+        """``F x`` (F object, u = image) or ``X f`` (X object, u = PSFs)."""
+        t, host = _to_device(u, self.device)
+        if self.__id__ == "F":
+            if t.dim() != 2:
+                raise IOError("Size missmatch between winaux and image size!")
+            if tuple(t.shape) != self.winaux.sx:
+                raise IOError("Size missmatch between winaux and image size!")
+            y = self.plan.forward_image(t, self.fft_gpu)
+        else:
+            if t.dim() != 3 or t.shape[0] != self.winaux.K:
+                raise IOError("Size missmatch between winaux and PSF size!")
+            y = self.plan.forward_psf(t, self.fft_gpu)
+        return y.cpu().numpy() if host else y
+
+    def cnvtp(self, y):
+        """``F^T y`` (image-shaped) or ``X^T y`` (PSF-stack-shaped)."""
+        if self.mode not in ("valid", "same"):
+            raise NotImplementedError("Not a valid mode!")
+        t, host = _to_device(y, self.device)
+        if self.__id__ == "F":
+            out, _ = self.plan.adjoint(t, fhat=self.fft_gpu, want_psf=False, adjoint=self.adjoint)
+        else:
+            _, out = self.plan.adjoint(t, xhat=self.fft_gpu, want_image=False, adjoint=self.adjoint)
+        return out.cpu().numpy() if host else out
