@@ -77,7 +77,6 @@ def algorithmic(w, wa, N):
         "forward": (px + pf + py, K * (3 * fft + prod)),
         # both adjoints: reads r, x, f, writes gx and gf; 4K FFTs + 2K products
         "adjoint": (py + px + pf + px + pf, K * (4 * fft + 2 * prod)),
-        "psf_spectrum": (pf + K * (N // 2 + 1) * N * 8, K * fft),
     }
 
 
@@ -150,17 +149,19 @@ def run_ours(args, rank, world, dev):
     fhat = plan.empty_spectrum()
     xhat = plan.empty_spectrum()
     y = torch.empty(plan.sy, device=dev)
-    r = torch.empty(plan.sy, device=dev)
     gx = torch.empty(plan.sx, device=dev)
     gf = torch.empty((K,) + plan.sf, device=dev)
-    loss = torch.empty((), device=dev)
+    loss = torch.empty((), dtype=torch.float64, device=dev)
 
     def step():
-        plan.psf_spectrum(f, out=fhat)
-        plan.forward_image(x, fhat, out=y, xhat_out=xhat)
-        torch.sub(y, y_obs, out=r)
-        torch.mul(0.5, torch.sum(r * r), out=loss)
-        plan.adjoint(r, fhat, xhat, gx=gx, gf=gf)
+        # fused forward (x, f -> y + both spectra) and fused adjoints of y - y_obs
+        plan.loss_grad(x, f, y_obs, loss=loss, gx=gx, gf=gf)
+
+    def k_forward():
+        plan.forward_both(x, f, out=y, xhat_out=xhat, fhat_out=fhat)
+
+    def k_adjoint():
+        plan.adjoint_residual(y, y_obs, fhat, xhat, loss=loss, gx=gx, gf=gf)
 
     flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
     stream = torch.cuda.Stream(device=dev)
@@ -197,27 +198,35 @@ def run_ours(args, rank, world, dev):
         clk = clocks.stop()
         t_ms = allreduce_max(t_ms, world, dev)
 
-        # per-kernel durations (eager launches, L2 flushed before each step)
-        names = ["psf_spectrum", "forward", "residual", "adjoint"]
-        acc = {n: 0.0 for n in names}
+        # per-kernel durations: each kernel (with its memsets) captured in its
+        # own graph, L2 flushed before each replay
+        k_forward()
+        k_adjoint()
+        torch.cuda.synchronize(dev)
+        kern_graphs = {}
+        for name, fn in (("forward", k_forward), ("adjoint", k_adjoint)):
+            gph = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(gph, stream=stream):
+                fn()
+            kern_graphs[name] = gph
+        torch.cuda.synchronize(dev)
+        kern_ms = {}
         reps = max(5, min(args.steps, 50))
-        for _ in range(reps):
-            flush.fill_(1.0)
-            ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
-            ev[0].record(stream)
-            plan.psf_spectrum(f, out=fhat)
-            ev[1].record(stream)
-            plan.forward_image(x, fhat, out=y, xhat_out=xhat)
-            ev[2].record(stream)
-            torch.sub(y, y_obs, out=r)
-            torch.mul(0.5, torch.sum(r * r), out=loss)
-            ev[3].record(stream)
-            plan.adjoint(r, fhat, xhat, gx=gx, gf=gf)
-            ev[4].record(stream)
-            torch.cuda.synchronize(dev)
-            for i, n in enumerate(names):
-                acc[n] += ev[i].elapsed_time(ev[i + 1])
-        kern_ms = {n: acc[n] / reps for n in names}
+        for name, gph in kern_graphs.items():
+            tot = 0.0
+            for i in range(reps + 2):
+                flush.fill_(1.0)
+                if name == "adjoint":
+                    k_forward()  # the adjoint reads what the forward leaves in L2
+                a = torch.cuda.Event(enable_timing=True)
+                b = torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                gph.replay()
+                b.record(stream)
+                torch.cuda.synchronize(dev)
+                if i >= 2:
+                    tot += a.elapsed_time(b)
+            kern_ms[name] = tot / reps
 
         # unfused per-stage comparator (torch ops + cuFFT), graph-captured
         from vmbd_gb300.unfused import UnfusedEff
@@ -256,7 +265,7 @@ def run_ours(args, rank, world, dev):
         hy = y_obs.cpu().pin_memory()
         ogx = torch.empty(plan.sx).pin_memory()
         ogf = torch.empty((K,) + plan.sf).pin_memory()
-        oloss = torch.empty(()).pin_memory()
+        oloss = torch.empty((), dtype=torch.float64).pin_memory()
 
         def e2e_step():
             x.copy_(hx, non_blocking=True)
@@ -282,10 +291,31 @@ def run_ours(args, rank, world, dev):
             et += a.elapsed_time(b)
         et = allreduce_max(et, world, dev)
     h2d = (hx.numel() + hf.numel() + hy.numel()) * 4
-    d2h = (ogx.numel() + ogf.numel()) * 4 + 4
+    d2h = (ogx.numel() + ogf.numel()) * 4 + 8
+    step()
+    k_forward()
+    torch.cuda.synchronize(dev)
     return dict(plan=plan, wa=wa, w=w, x_np=x_np, f_np=f_np, y_obs=y_obs.cpu().numpy(),
                 gx=gx.cpu().numpy(), gf=gf.cpu().numpy(), y=y.cpu().numpy(), t_ms=t_ms,
                 kern_ms=kern_ms, unfused_ms=unfused_ms, e2e_ms=et, h2d=h2d, d2h=d2h, clocks=clk)
+
+
+def profile_run(args, dev):
+    """The step, eagerly, warmup + steps times (no graph, no comparators)."""
+    import torch
+    from vmbd_gb300.eff import EffPlan
+    w = WORKLOADS[args.workload]
+    wa, x_np, f_np = make_inputs(w, seed=0)
+    plan = EffPlan(wa, w["sf"], "valid", device=dev)
+    x = torch.from_numpy(x_np).to(dev)
+    f = torch.from_numpy(f_np).to(dev)
+    y_obs = plan.forward_image(x, plan.psf_spectrum(f))
+    flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    for _ in range(args.warmup + args.steps):
+        flush.fill_(1.0)
+        plan.loss_grad(x, f, y_obs)
+    torch.cuda.synchronize(dev)
+    print(json.dumps({"profile": args.workload, "steps": args.steps, "warmup": args.warmup}))
 
 
 def barrier(world):
@@ -304,18 +334,21 @@ def allreduce_max(v, world, dev):
     return float(t.item())
 
 
-def oracle_step(w, wa, x, f, y_obs):
-    """One fwd + both exact adjoints of the FP64 oracle."""
+def oracle_step(w, wa, x, f, y_obs, r=None):
+    """One fwd + both exact adjoints of the FP64 oracle (of residual ``r``
+    when given, else of its own ``y - y_obs``)."""
     from oracle import eff64
     g = eff64.Geometry(w["sx"], w["sf"], wa.csf, wa.sw, wa.nhop, "valid")
     ws = wa.ws.astype(np.float64)
     y = eff64.forward(x, f, g, ws)
-    r = y - y_obs
+    if r is None:
+        r = y - y_obs
     return y, eff64.adjoint_image(r, f, g, ws), eff64.adjoint_psf(r, x, g, ws)
 
 
-def cpu_sample(w, wa, x, f, y_obs, budget_s=12.0, max_reps=50, warm=1):
-    """Time the oracle step on the host (scipy.fft over all cores)."""
+def cpu_sample(w, wa, x, f, y_obs, r_gpu, budget_s=12.0, max_reps=50, warm=1):
+    """Time the oracle step on the host (scipy.fft over all cores); the last
+    run's adjoints take the GPU's residual so that they check the kernels."""
     from oracle import eff64
     cores = os.cpu_count() or 1
     eff64.set_fft_workers(cores)
@@ -325,8 +358,9 @@ def cpu_sample(w, wa, x, f, y_obs, budget_s=12.0, max_reps=50, warm=1):
     t_end = time.perf_counter() + budget_s
     while len(times) < max_reps and (not times or time.perf_counter() < t_end):
         t0 = time.perf_counter()
-        out = oracle_step(w, wa, x, f, y_obs)
+        oracle_step(w, wa, x, f, y_obs)
         times.append(time.perf_counter() - t0)
+    out = oracle_step(w, wa, x, f, y_obs, r=r_gpu)
     return statistics.median(times), len(times), cores, out
 
 
@@ -338,6 +372,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=list(WORKLOADS), default="cfg2")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", action="store_true",
+                    help="short eager run of the step only (for an ncu launch list / capture)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -347,8 +383,8 @@ def main():
     w = WORKLOADS[args.workload]
     pixels = w["sx"][0] * w["sx"][1]
     metric = "EFF fwd+adjoint Mpixel/s"
-    config = {"workload": args.workload, "desc": w["desc"], "step": "psf spectrum + fused forward + "
-              "residual/loss + fused adjoint (both gradients)", "images_per_gpu": 1,
+    config = {"workload": args.workload, "desc": w["desc"], "step": "fused forward (x, f -> y, "
+              "both spectra) + fused adjoint of y - y_obs (loss, both gradients)", "images_per_gpu": 1,
               "l2": "flushed (256 MB write) before every timed step", "parallelism": f"replicas x{world}"}
 
     if args.impl == "reference":
@@ -386,6 +422,9 @@ def main():
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
+    if args.profile:
+        profile_run(args, dev)
+        return
     R = run_ours(args, rank, world, dev)
     plan, wa = R["plan"], R["wa"]
     ms = R["t_ms"] / args.steps
@@ -420,11 +459,12 @@ def main():
                         "speedup": R["unfused_ms"] / ms},
         "e2e": {"value": world * pixels / (e2e_ms * 1e-3) / 1e6, "unit": "Mpixel/s",
                 "ms_per_step": e2e_ms, "h2d_bytes_per_step": R["h2d"], "d2h_bytes_per_step": R["d2h"]},
-        "gpu_launches": 3 * args.steps,
+        "gpu_launches": 2 * args.steps,
         "clocks": clk,
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        t_cpu, reps, cores, (y_o, gx_o, gf_o) = cpu_sample(w, wa, R["x_np"], R["f_np"], R["y_obs"])
+        r_gpu = R["y"].astype(np.float64) - R["y_obs"]
+        t_cpu, reps, cores, (y_o, gx_o, gf_o) = cpu_sample(w, wa, R["x_np"], R["f_np"], R["y_obs"], r_gpu)
         line["cpu_baseline"] = {"value": pixels / t_cpu / 1e6, "unit": "Mpixel/s", "cores": cores,
                                 "kind": "port",
                                 "sample": f"{reps} full-image steps of the same workload (FP64 NumPy "
@@ -433,7 +473,8 @@ def main():
         def rel(a, b):
             return float(np.linalg.norm(np.asarray(a, np.float64) - b) / np.linalg.norm(b))
         line["rel_l2_vs_fp64_oracle"] = {"forward": rel(R["y"], y_o), "adjoint_image": rel(R["gx"], gx_o),
-                                         "adjoint_psf": rel(R["gf"], gf_o)}
+                                         "adjoint_psf": rel(R["gf"], gf_o),
+                                         "note": "adjoints of the same residual y_gpu - y_obs"}
     if rank == 0:
         print(json.dumps(line))
     if world > 1:

@@ -97,6 +97,30 @@ int eff_forward_psf(const EffPlan* plan, const float* f, const void* xhat, float
 int eff_adjoint(const EffPlan* plan, const float* y, const void* fhat, const void* xhat, float* gx,
                 float* gf, int adj_mode, int batch, void* stream);
 
+/* y = EFF(x, f) from the raw image and PSFs in one kernel (the forward of an
+ * autograd step): both operands are transformed in-kernel.  xhat_out /
+ * fhat_out (nullable) receive the two spectra for a later eff_adjoint. */
+int eff_forward_both(const EffPlan* plan, const float* x, const float* f, float* y, void* xhat_out,
+                     void* fhat_out, int batch, void* stream);
+
+/* eff_adjoint of the residual r = y - y_obs (both [batch, sy0, sy1]) without
+ * forming r; loss (nullable, double [batch]) receives 0.5 * ||y - y_obs||^2.
+ * The gradient of that loss w.r.t. x and f (cnvinv_objfun/gradfun without
+ * regularisation, olaGPU.py:756-811). */
+int eff_adjoint_residual(const EffPlan* plan, const float* y, const float* y_obs, const void* fhat,
+                         const void* xhat, float* gx, float* gf, double* loss, int adj_mode,
+                         int batch, void* stream);
+
+/* One loss/gradient step of 0.5 * ||EFF(x, f) - y_obs||^2: eff_forward_both
+ * then eff_adjoint_residual (exact adjoints), with the forward output and
+ * the two spectra in a caller-provided device workspace of at least
+ * eff_loss_grad_workspace_bytes(plan, batch) bytes.  gx or gf may be NULL
+ * (not both); loss may be NULL. */
+size_t eff_loss_grad_workspace_bytes(const EffPlan* plan, int batch);
+int eff_loss_grad(const EffPlan* plan, const float* x, const float* f, const float* y_obs,
+                  double* loss, float* gx, float* gf, void* workspace, size_t workspace_bytes,
+                  int batch, void* stream);
+
 /* PSF projections on [K, n] stacks (n = sf0*sf1), in place.
  * EFF_PROJ_CLIP_NORMALIZE: f = max(f, 0) then f /= sum(f) when sum > 1e-6
  *   (L-BFGS-B bounds olaGPU.py:404-411 + normalize gputools.py:1025-1044).

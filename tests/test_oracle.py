@@ -169,3 +169,37 @@ def test_synthetic_generators():
     assert np.array_equal(synth.blob_edge_image((32, 32), 7), synth.blob_edge_image((32, 32), 7))
     d = synth.drifting_motion_psfs(4, 3, (25, 25), seed=2)
     assert d.shape == (4, 3, 25, 25)
+
+
+def test_fp64_finite_differences():
+    """Central differences (h = 1e-3, 200 coordinates) of 0.5||EFF(x,f)-y||^2
+    in FP64 against the exact adjoints."""
+    g, ws = small_geom("valid")
+    rng = np.random.default_rng(6)
+    x = rng.random(g.sx)
+    f = rng.random((g.K,) + g.sf)
+    y = rng.random(g.sy)
+    res = eff64.forward(x, f, g, ws) - y
+    gx = eff64.adjoint_image(res, f, g, ws)
+    gf = eff64.adjoint_psf(res, x, g, ws)
+
+    def L(xv, fv):
+        return 0.5 * np.sum((eff64.forward(xv, fv, g, ws) - y) ** 2)
+
+    h = 1e-3
+    fd, an = [], []
+    for _ in range(100):
+        i = tuple(int(rng.integers(0, s)) for s in g.sx)
+        xp, xm = x.copy(), x.copy()
+        xp[i] += h
+        xm[i] -= h
+        fd.append((L(xp, f) - L(xm, f)) / (2 * h))
+        an.append(gx[i])
+    for _ in range(100):
+        i = tuple(int(rng.integers(0, s)) for s in (g.K,) + g.sf)
+        fp, fm = f.copy(), f.copy()
+        fp[i] += h
+        fm[i] -= h
+        fd.append((L(x, fp) - L(x, fm)) / (2 * h))
+        an.append(gf[i])
+    assert rel(np.array(fd), np.array(an)) < 1e-8

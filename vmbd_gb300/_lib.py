@@ -26,6 +26,7 @@ EXPORTS = (
     "eff_plan_create", "eff_plan_destroy", "eff_plan_frame", "eff_spectrum_bytes",
     "eff_psf_spectrum", "eff_image_spectrum", "eff_forward_image", "eff_forward_psf",
     "eff_adjoint", "eff_project_psf", "eff_basis_project", "eff_last_error",
+    "eff_forward_both", "eff_adjoint_residual", "eff_loss_grad_workspace_bytes", "eff_loss_grad",
 )
 
 
@@ -72,6 +73,10 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "eff_project_psf": ([fp, ip, ip, ip, vp], ip),
         "eff_basis_project": ([fp, fp, fp, ip, ip, vp], ip),
         "eff_last_error": ([], ctypes.c_char_p),
+        "eff_forward_both": ([vp, fp, fp, fp, vp, vp, ip, vp], ip),
+        "eff_adjoint_residual": ([vp, fp, fp, vp, vp, fp, fp, vp, ip, ip, vp], ip),
+        "eff_loss_grad_workspace_bytes": ([vp, ip], ctypes.c_size_t),
+        "eff_loss_grad": ([vp, fp, fp, fp, vp, fp, fp, vp, ctypes.c_size_t, ip, vp], ip),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)

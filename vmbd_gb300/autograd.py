@@ -1,8 +1,8 @@
 """``torch.autograd.Function`` for the EFF operator.
 
-Forward: ``y = EFF(x, f)`` -- one spectrum kernel for the PSFs, one fused
-forward kernel for the image that also leaves the windowed-patch spectrum
-behind.  Backward: one fused adjoint kernel computes both ``F^T g`` and
+Forward: ``y = EFF(x, f)`` -- one fused kernel that transforms the
+windowed patches and the PSFs, multiplies, inverse transforms and
+overlap-adds, leaving both spectra behind.  Backward: one fused adjoint kernel computes both ``F^T g`` and
 ``X^T g`` from a single transform of the incoming gradient, reusing both
 cached spectra (the two cnvtp calls of olaGPU.py:261-311 that blind
 deconvolution needs: image step and PSF step).
@@ -17,9 +17,10 @@ from .eff import EffPlan
 class EFFFunction(torch.autograd.Function):
     @staticmethod
     def forward(ctx, x, f, plan: EffPlan):
-        fhat = plan.psf_spectrum(f.detach())
-        xhat = plan.empty_spectrum(x.shape[0] if x.dim() == 3 else None)
-        y = plan.forward_image(x.detach(), fhat, xhat_out=xhat)
+        batch = x.shape[0] if x.dim() == 3 else None
+        fhat = plan.empty_spectrum(batch)
+        xhat = plan.empty_spectrum(batch)
+        y = plan.forward_both(x.detach(), f.detach(), xhat_out=xhat, fhat_out=fhat)
         ctx.plan = plan
         ctx.fhat = fhat
         ctx.xhat = xhat

@@ -36,6 +36,7 @@ struct EffPlan {
 namespace {
 
 thread_local std::string g_last_error;
+constexpr size_t kSmemLimit = 227u * 1024u;
 
 int fail(int code, const std::string& msg) {
   g_last_error = msg;
@@ -73,7 +74,7 @@ eff::Params base_params(const EffPlan* p) {
 
 int run(const EffPlan* p, int op, const eff::Params& P, int batch, void* stream) {
   const size_t smem = eff::smem_bytes(p->N, op, P, p->threads);
-  if (smem > 227u * 1024u)
+  if (smem > kSmemLimit)
     return fail(EFF_ERR_UNSUPPORTED, "frame needs " + std::to_string(smem) + " bytes of shared memory");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   cudaError_t e;
@@ -91,6 +92,80 @@ int check_plan(const EffPlan* p, int batch) {
   if (!p) return fail(EFF_ERR_INVALID, "null plan");
   if (batch < 1 || batch > 65535) return fail(EFF_ERR_INVALID, "batch must be in [1, 65535]");
   return EFF_OK;
+}
+
+int adjoint_impl(const EffPlan* plan, const float* y, const float* y_obs, const void* fhat,
+                 const void* xhat, float* gx, float* gf, double* loss, int adj_mode, int batch,
+                 void* stream) {
+  if (int s = check_plan(plan, batch)) return s;
+  if (!y || (!gx && !gf)) return fail(EFF_ERR_INVALID, "null argument");
+  if (gx && !fhat) return fail(EFF_ERR_INVALID, "image adjoint needs the PSF spectrum");
+  if (gf && !xhat) return fail(EFF_ERR_INVALID, "PSF adjoint needs the image spectrum");
+  if (adj_mode != EFF_ADJ_EXACT && adj_mode != EFF_ADJ_REFERENCE)
+    return fail(EFF_ERR_INVALID, "adj_mode");
+  if (adj_mode == EFF_ADJ_REFERENCE && plan->g.mode == EFF_MODE_FULL)
+    return fail(EFF_ERR_INVALID, "Not a valid mode!");  // olaGPU.py:285-286
+  eff::Params P = base_params(plan);
+  P.y = y;
+  P.y_obs = y_obs;
+  P.b0 = static_cast<const float2*>(fhat);
+  P.b1 = static_cast<const float2*>(xhat);
+  P.out0 = gx;
+  P.out1 = gf;
+  P.loss = loss;
+  P.out0_bs = P.x_bs;
+  P.out1_bs = P.f_bs;
+  if (adj_mode == EFF_ADJ_REFERENCE) {
+    // chop_pad_GPU at offset `off`, extent sw (olaGPU.py:276-286).
+    P.lo0 = plan->off[0];
+    P.hi0 = plan->off[0] + plan->g.sw[0] < plan->E[0] ? plan->off[0] + plan->g.sw[0] : plan->E[0];
+    P.lo1 = plan->off[1];
+    P.hi1 = plan->off[1] + plan->g.sw[1] < plan->E[1] ? plan->off[1] + plan->g.sw[1] : plan->E[1];
+  }
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (gx) {
+    cudaError_t e = cudaMemsetAsync(gx, 0, sizeof(float) * P.x_bs * batch, st);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+  }
+  if (loss) {
+    cudaError_t e = cudaMemsetAsync(loss, 0, sizeof(double) * batch, st);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+  }
+  return run(plan, eff::OP_ADJ, P, batch, stream);
+}
+
+// Workspace of the fused loss/gradient step: the two cached spectra and the
+// forward output, each 256-byte aligned.
+struct Workspace {
+  size_t xhat, fhat, y, total;
+};
+
+Workspace workspace_layout(const EffPlan* p, int batch) {
+  auto up = [](size_t v) { return (v + 255) & ~size_t(255); };
+  const size_t spec = sizeof(float2) * (size_t)p->K * (p->N / 2 + 1) * p->N * batch;
+  const size_t ybytes = sizeof(float) * (size_t)p->sy[0] * p->sy[1] * batch;
+  Workspace w;
+  w.xhat = 0;
+  w.fhat = up(spec);
+  w.y = w.fhat + up(spec);
+  w.total = w.y + up(ybytes);
+  return w;
+}
+
+// Forward from raw (x, f) leaving both spectra in the workspace, then both
+// adjoints of the residual y - y_obs with the loss 0.5 * ||y - y_obs||^2.
+int loss_grad_impl(const EffPlan* plan, const float* x, const float* f, const float* y_obs,
+                   double* loss, float* gx, float* gf, char* ws, int batch, void* stream) {
+  if (!x || !f || !y_obs) return fail(EFF_ERR_INVALID, "null argument");
+  if (!gx && !gf) return fail(EFF_ERR_INVALID, "eff_loss_grad needs gx or gf");
+  const Workspace w = workspace_layout(plan, batch);
+  float2* xhat = reinterpret_cast<float2*>(ws + w.xhat);
+  float2* fhat = reinterpret_cast<float2*>(ws + w.fhat);
+  float* y = reinterpret_cast<float*>(ws + w.y);
+  int s = eff_forward_both(plan, x, f, y, gf ? xhat : nullptr, gx ? fhat : nullptr, batch, stream);
+  if (s != EFF_OK) return s;
+  return adjoint_impl(plan, y, y_obs, gx ? fhat : nullptr, gf ? xhat : nullptr, gx, gf, loss,
+                      EFF_ADJ_EXACT, batch, stream);
 }
 
 }  // namespace
@@ -136,19 +211,22 @@ int eff_plan_create(const EffGeom* geom, const float* win0, const float* win1, E
                                          std::to_string(emax) + ")");
   if (p.N < emax) return fail(EFF_ERR_INVALID, "FFT frame smaller than sw + sf - 1");
 
-  // Threads per CTA: 256, or 128 when the frame plus exchange scratch would
-  // not fit in shared memory otherwise.
-  p.threads = 256;
+  // Threads per CTA: the most the kernels are compiled for, halved while the
+  // frame plus the per-group exchange scratch would not fit in shared memory.
+  p.threads = eff::max_threads(p.N);
   {
     eff::Params P = base_params(&p);
     P.out0 = reinterpret_cast<float*>(1);
     P.out1 = reinterpret_cast<float*>(1);
-    size_t worst = 0;
-    for (int op = 0; op <= 4; ++op) {
-      const size_t s = eff::smem_bytes(p.N, op, P, 256);
-      if (s > worst) worst = s;
+    for (;;) {
+      size_t worst = 0;
+      for (int op = 0; op < eff::kNumOps; ++op) {
+        const size_t s = eff::smem_bytes(p.N, op, P, p.threads);
+        if (s > worst) worst = s;
+      }
+      if (worst <= kSmemLimit || p.threads <= 64) break;
+      p.threads /= 2;
     }
-    if (worst > 227u * 1024u) p.threads = 128;
   }
 
   cudaError_t e = cudaGetDevice(&p.device);
@@ -262,34 +340,46 @@ int eff_forward_psf(const EffPlan* plan, const float* f, const void* xhat, float
 
 int eff_adjoint(const EffPlan* plan, const float* y, const void* fhat, const void* xhat, float* gx,
                 float* gf, int adj_mode, int batch, void* stream) {
+  return adjoint_impl(plan, y, nullptr, fhat, xhat, gx, gf, nullptr, adj_mode, batch, stream);
+}
+
+int eff_adjoint_residual(const EffPlan* plan, const float* y, const float* y_obs, const void* fhat,
+                         const void* xhat, float* gx, float* gf, double* loss, int adj_mode,
+                         int batch, void* stream) {
+  if (!y_obs) return fail(EFF_ERR_INVALID, "null y_obs");
+  return adjoint_impl(plan, y, y_obs, fhat, xhat, gx, gf, loss, adj_mode, batch, stream);
+}
+
+int eff_forward_both(const EffPlan* plan, const float* x, const float* f, float* y, void* xhat_out,
+                     void* fhat_out, int batch, void* stream) {
   if (int s = check_plan(plan, batch)) return s;
-  if (!y || (!gx && !gf)) return fail(EFF_ERR_INVALID, "null argument");
-  if (gx && !fhat) return fail(EFF_ERR_INVALID, "image adjoint needs the PSF spectrum");
-  if (gf && !xhat) return fail(EFF_ERR_INVALID, "PSF adjoint needs the image spectrum");
-  if (adj_mode != EFF_ADJ_EXACT && adj_mode != EFF_ADJ_REFERENCE)
-    return fail(EFF_ERR_INVALID, "adj_mode");
-  if (adj_mode == EFF_ADJ_REFERENCE && plan->g.mode == EFF_MODE_FULL)
-    return fail(EFF_ERR_INVALID, "Not a valid mode!");  // olaGPU.py:285-286
+  if (!x || !f || !y) return fail(EFF_ERR_INVALID, "null argument");
   eff::Params P = base_params(plan);
-  P.y = y;
-  P.b0 = static_cast<const float2*>(fhat);
-  P.b1 = static_cast<const float2*>(xhat);
-  P.out0 = gx;
-  P.out1 = gf;
-  P.out0_bs = P.x_bs;
-  P.out1_bs = P.f_bs;
-  if (adj_mode == EFF_ADJ_REFERENCE) {
-    // chop_pad_GPU at offset `off`, extent sw (olaGPU.py:276-286).
-    P.lo0 = plan->off[0];
-    P.hi0 = plan->off[0] + plan->g.sw[0] < plan->E[0] ? plan->off[0] + plan->g.sw[0] : plan->E[0];
-    P.lo1 = plan->off[1];
-    P.hi1 = plan->off[1] + plan->g.sw[1] < plan->E[1] ? plan->off[1] + plan->g.sw[1] : plan->E[1];
-  }
-  if (gx) {
-    cudaError_t e = cudaMemsetAsync(gx, 0, sizeof(float) * P.x_bs * batch, static_cast<cudaStream_t>(stream));
-    if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
-  }
-  return run(plan, eff::OP_ADJ, P, batch, stream);
+  P.x = x;
+  P.f = f;
+  P.out0 = y;
+  P.out0_bs = P.y_bs;
+  P.a_out = static_cast<float2*>(xhat_out);
+  P.b_out = static_cast<float2*>(fhat_out);
+  cudaError_t e = cudaMemsetAsync(y, 0, sizeof(float) * P.y_bs * batch, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+  return run(plan, eff::OP_FWD_BOTH, P, batch, stream);
+}
+
+size_t eff_loss_grad_workspace_bytes(const EffPlan* plan, int batch) {
+  if (!plan || batch < 1) return 0;
+  return workspace_layout(plan, batch).total;
+}
+
+int eff_loss_grad(const EffPlan* plan, const float* x, const float* f, const float* y_obs,
+                  double* loss, float* gx, float* gf, void* workspace, size_t workspace_bytes,
+                  int batch, void* stream) {
+  if (int s = check_plan(plan, batch)) return s;
+  if (!workspace) return fail(EFF_ERR_INVALID, "null workspace");
+  const Workspace w = workspace_layout(plan, batch);
+  if (workspace_bytes < w.total)
+    return fail(EFF_ERR_INVALID, "workspace too small: need " + std::to_string(w.total) + " bytes");
+  return loss_grad_impl(plan, x, f, y_obs, loss, gx, gf, static_cast<char*>(workspace), batch, stream);
 }
 
 int eff_project_psf(float* f, int K, int n, int proj_mode, void* stream) {

@@ -5,15 +5,15 @@
 // (N/2+1 bins per row) in shared memory:
 //
 //  1. row pass (R2C): pairs of real operand rows are read straight from HBM
-//     (windowed image patch, PSF, or the output-side image for the adjoints),
-//     packed as one complex row, transformed, and split into two half-spectrum
-//     rows.
+//     (windowed image patch, PSF, or the output-side image / residual for the
+//     adjoints), packed as one complex row, transformed, and split into two
+//     half-spectrum rows.  Kernels with two operands run both in one loop.
 //  2. column pass: each lane group takes one column (columns 0 and N/2, both
 //     real after the row pass, share one complex transform), transforms it,
-//     optionally stores it as a cached spectrum, multiplies it by the cached
-//     spectrum of the other operand (conjugated for the adjoints) and inverse
-//     transforms it, all in registers; only the rows the epilogue needs go
-//     back to shared memory.
+//     optionally stores it as a cached spectrum, multiplies it by the other
+//     operand's spectrum (conjugated for the adjoints) and inverse transforms
+//     it, all in registers; only the rows the epilogue needs go back to
+//     shared memory.
 //  3. row pass (C2R): pairs of half-spectrum rows are inverse transformed as
 //     one complex row; the epilogue overlap-adds into the output image with
 //     fp32 atomics (forward: full-convolution extent, cropped by mode; image
@@ -28,10 +28,14 @@ namespace eff {
 enum Op : int {
   OP_SPEC_IMAGE = 0,  // X-hat of the windowed patches (OlaGPU X object, olaGPU.py:147-157)
   OP_SPEC_PSF = 1,    // F-hat of the PSFs (OlaGPU F object, olaGPU.py:142-157)
-  OP_FWD_IMAGE = 2,   // y = F x   (F.cnv(x), olaGPU.py:200-257)
-  OP_FWD_PSF = 3,     // y = X f   (X.cnv(f), olaGPU.py:188-193, 219-257)
-  OP_ADJ = 4,         // F^T y and/or X^T y (cnvtp, olaGPU.py:261-311)
+  OP_FWD_IMAGE = 2,   // y = F x, F given by F-hat (F.cnv(x), olaGPU.py:200-257)
+  OP_FWD_PSF = 3,     // y = X f, X given by X-hat (X.cnv(f), olaGPU.py:188-193, 219-257)
+  OP_FWD_BOTH = 4,    // y = EFF(x, f) from raw x and f; leaves X-hat and F-hat behind
+  OP_ADJ = 5,         // F^T r and/or X^T r (cnvtp, olaGPU.py:261-311), r = y or y - y_obs
 };
+constexpr int kNumOps = 6;
+
+enum Operand : int { OPND_IMAGE = 0, OPND_PSF = 1, OPND_RESID = 2 };
 
 struct Params {
   int sx0, sx1, sf0, sf1, csf0, csf1, sw0, sw1, hop0, hop1;
@@ -40,11 +44,14 @@ struct Params {
   const float* x;          // image [sx0, sx1]
   const float* f;          // PSFs [K, sf0, sf1]
   const float* y;          // output-side image [sy0, sy1] (adjoint input)
+  const float* y_obs;      // adjoint: when set, the input is y - y_obs
   const float2* b0;        // cached spectrum: F-hat (fwd image / adj image) or X-hat (fwd psf)
   const float2* b1;        // cached spectrum: X-hat (adj psf)
-  float2* a_out;           // spectrum of this kernel's operand (optional)
+  float2* a_out;           // spectrum of operand A (optional)
+  float2* b_out;           // spectrum of operand B (OP_FWD_BOTH, optional)
   float* out0;             // y (forward) or gx (image adjoint)
   float* out1;             // gf (PSF adjoint)
+  double* loss;            // adjoint with y_obs: += 0.5 * sum (y - y_obs)^2 (optional)
   const float2* win0;      // window factors (alpha, gamma) [csf0, sw0]
   const float2* win1;      // window factors (alpha, gamma) [csf1, sw1]
   const float2* tw;        // W_N table [16*G]
@@ -52,6 +59,30 @@ struct Params {
 };
 
 __host__ __device__ constexpr int frame_pitch(int N) { return N / 2 + 1; }
+__host__ __device__ constexpr int even_up(int v) { return (v + 1) & ~1; }
+// Threads per CTA the kernel is compiled for (the host may launch fewer).
+__host__ __device__ constexpr int max_threads(int N) { return N >= 256 ? 256 : 512; }
+
+// Operand A / B of each op, their row counts and frame bases.
+__host__ __device__ constexpr int opnd_a(int op) {
+  return (op == OP_SPEC_PSF || op == OP_FWD_PSF) ? OPND_PSF : (op == OP_ADJ ? OPND_RESID : OPND_IMAGE);
+}
+__host__ __device__ constexpr bool has_b(int op) { return op == OP_FWD_BOTH; }
+
+__host__ __device__ inline int opnd_rows(const Params& P, int kind) {
+  return kind == OPND_IMAGE ? P.sw0 : (kind == OPND_PSF ? P.sf0 : P.E0);
+}
+
+// Frame rows a CTA uses (the host sizes shared memory with the same formula).
+__host__ __device__ inline int frame_rows(const Params& P, int op) {
+  const int ra = even_up(opnd_rows(P, opnd_a(op)));
+  if (op == OP_SPEC_IMAGE || op == OP_SPEC_PSF) return ra;
+  if (op == OP_FWD_IMAGE || op == OP_FWD_PSF) return max(ra, even_up(P.E0));
+  if (op == OP_FWD_BOTH) return max(ra + even_up(P.sf0), even_up(P.E0));
+  const int r0 = P.out0 ? even_up(P.sw0) : 0;
+  const int r1 = P.out1 ? even_up(P.sf0) : 0;
+  return max(ra, r0 + r1);
+}
 
 template <int N>
 __device__ __forceinline__ unsigned group_mask(int lane) {
@@ -68,108 +99,94 @@ __device__ __forceinline__ float window_weight(float2 u, float2 v) {
   return (u.x < 0.f || v.x < 0.f) ? u.y * v.y : u.x * v.x;
 }
 
-// Operand value at frame position (r, c) of patch (m, n) / index k.
-template <int OP>
-__device__ __forceinline__ float operand(const Params& P, const float* x, const float* f,
-                                         const float* y, int m, int n, int k, int r, int c) {
-  if constexpr (OP == OP_SPEC_IMAGE || OP == OP_FWD_IMAGE) {
+struct Patch {
+  int m, n, k;
+  const float* x;
+  const float* f;
+  const float* y;
+  const float* y_obs;
+};
+
+// Operand value at frame position (r, c).
+template <int KIND>
+__device__ __forceinline__ float operand(const Params& P, const Patch& T, int r, int c) {
+  if constexpr (KIND == OPND_IMAGE) {
     if (r >= P.sw0 || c >= P.sw1) return 0.f;
-    const int i = m * P.hop0 + r, j = n * P.hop1 + c;
+    const int i = T.m * P.hop0 + r, j = T.n * P.hop1 + c;
     if (i >= P.sx0 || j >= P.sx1) return 0.f;
-    return window_weight(__ldg(P.win0 + m * P.sw0 + r), __ldg(P.win1 + n * P.sw1 + c)) *
-           __ldg(x + (long long)i * P.sx1 + j);
-  } else if constexpr (OP == OP_SPEC_PSF || OP == OP_FWD_PSF) {
+    return window_weight(__ldg(P.win0 + T.m * P.sw0 + r), __ldg(P.win1 + T.n * P.sw1 + c)) *
+           __ldg(T.x + (long long)i * P.sx1 + j);
+  } else if constexpr (KIND == OPND_PSF) {
     if (r >= P.sf0 || c >= P.sf1) return 0.f;
-    return __ldg(f + ((long long)k * P.sf0 + r) * P.sf1 + c);
+    return __ldg(T.f + ((long long)T.k * P.sf0 + r) * P.sf1 + c);
   } else {
     if (r < P.lo0 || r >= P.hi0 || c < P.lo1 || c >= P.hi1) return 0.f;
-    const int i = m * P.hop0 + r - P.off0, j = n * P.hop1 + c - P.off1;
+    const int i = T.m * P.hop0 + r - P.off0, j = T.n * P.hop1 + c - P.off1;
     if (i < 0 || j < 0 || i >= P.sy0 || j >= P.sy1) return 0.f;
-    return __ldg(y + (long long)i * P.sy1 + j);
+    const long long o = (long long)i * P.sy1 + j;
+    float v = __ldg(T.y + o);
+    if (T.y_obs) v -= __ldg(T.y_obs + o);
+    return v;
   }
 }
 
-template <int OP>
-__device__ __forceinline__ int operand_rows(const Params& P) {
-  if constexpr (OP == OP_SPEC_IMAGE || OP == OP_FWD_IMAGE) return P.sw0;
-  else if constexpr (OP == OP_SPEC_PSF || OP == OP_FWD_PSF) return P.sf0;
-  else return P.E0;
-}
-
-// Phase 1: real operand rows -> half-spectrum rows [0, even(rows)).
-template <int N, int OP>
-__device__ __forceinline__ void row_r2c(const Params& P, const float* x, const float* f,
-                                        const float* y, int m, int n, int k, float2* frame,
-                                        float2* scr, const float2* tw, int gid, int NG, int g,
-                                        unsigned gmask) {
+// R2C of one pair of operand rows (ra, ra+1) into frame rows base+ra, base+ra+1.
+template <int N, int KIND>
+__device__ __forceinline__ void r2c_unit(const Params& P, const Patch& T, int ra, float2* frame,
+                                         int base, float2* scr, const float2* tw, int g,
+                                         unsigned gmask) {
   constexpr int G = FftShape<N>::G;
   constexpr int HP = frame_pitch(N);
-  const int rows = operand_rows<OP>(P);
-  const int nunits = (rows + 1) >> 1;
-  for (int u = gid; u < nunits; u += NG) {
-    const int ra = 2 * u, rb = ra + 1;
-    float2 v[16];
+  float2 v[16];
 #pragma unroll
-    for (int mm = 0; mm < 16; ++mm) {
-      const int c = g + G * mm;
-      v[mm] = make_float2(operand<OP>(P, x, f, y, m, n, k, ra, c),
-                          operand<OP>(P, x, f, y, m, n, k, rb, c));
-    }
-    fft_fwd<N>(v, g, scr, tw, gmask);
-    float2 p[16];
-    hermitian_partner<N>(v, p, g, gmask);
+  for (int mm = 0; mm < 16; ++mm) {
+    const int c = g + G * mm;
+    v[mm] = make_float2(operand<KIND>(P, T, ra, c), operand<KIND>(P, T, ra + 1, c));
+  }
+  fft_fwd<N>(v, g, scr, tw, gmask);
+  float2 p[16];
+  hermitian_partner<N>(v, p, g, gmask);
+  float2* rowa = frame + (base + ra) * HP;
+  float2* rowb = rowa + HP;
 #pragma unroll
-    for (int j = 0; j <= 8; ++j) {
-      if (j == 8 && g != 0) break;
-      const int kk = g + G * j;
-      frame[ra * HP + kk] = make_float2(0.5f * (v[j].x + p[j].x), 0.5f * (v[j].y - p[j].y));
-      frame[rb * HP + kk] = make_float2(0.5f * (v[j].y + p[j].y), 0.5f * (p[j].x - v[j].x));
-    }
+  for (int j = 0; j <= 8; ++j) {
+    if (j == 8 && g != 0) break;
+    const int kk = g + G * j;
+    rowa[kk] = make_float2(0.5f * (v[j].x + p[j].x), 0.5f * (v[j].y - p[j].y));
+    rowb[kk] = make_float2(0.5f * (v[j].y + p[j].y), 0.5f * (p[j].x - v[j].x));
   }
 }
 
-// Phase 3: half-spectrum rows [base, base+nrows) -> real rows, fed to epi(r, c, value).
-template <int N, class Epi>
-__device__ __forceinline__ void row_c2r(float2* frame, int base, int nrows, int ncols,
-                                        float2* scr, const float2* tw, int gid, int NG, int g,
-                                        unsigned gmask, Epi epi) {
-  constexpr int G = FftShape<N>::G;
-  constexpr int HP = frame_pitch(N);
-  const int nunits = (nrows + 1) >> 1;
-  for (int u = gid; u < nunits; u += NG) {
-    const int ra = base + 2 * u, rb = ra + 1;
-    float2 v[16];
-#pragma unroll
-    for (int j = 0; j < 16; ++j) {
-      const int kk = g + G * j;
-      float2 ya, yb;
-      if (j < 8 || (j == 8 && g == 0)) {
-        ya = frame[ra * HP + kk];
-        yb = frame[rb * HP + kk];
-      } else {
-        ya = frame[ra * HP + (N - kk)];
-        yb = frame[rb * HP + (N - kk)];
-        ya.y = -ya.y;
-        yb.y = -yb.y;
-      }
-      v[j] = make_float2(ya.x - yb.y, ya.y + yb.x);
-    }
-    fft_inv<N>(v, g, scr, tw, gmask);
-    const bool has_b = (2 * u + 1) < nrows;
-#pragma unroll
-    for (int mm = 0; mm < 16; ++mm) {
-      const int c = g + G * mm;
-      if (c < ncols) {
-        epi(2 * u, c, v[mm].x);
-        if (has_b) epi(2 * u + 1, c, v[mm].y);
-      }
-    }
-  }
-}
-
-// Load column unit u (u == 0: columns 0 and N/2 packed) of rows [0, rows).
+// C2R of frame rows (ra, ra+1); returns real row ra in .x, ra+1 in .y,
+// layout A (register m holds column g + G*m).
 template <int N>
-__device__ __forceinline__ void load_column(const float2* frame, int u, int rows, int g,
+__device__ __forceinline__ void c2r_unit(const float2* frame, int ra, float2 (&v)[16], float2* scr,
+                                         const float2* tw, int g, unsigned gmask) {
+  constexpr int G = FftShape<N>::G;
+  constexpr int HP = frame_pitch(N);
+  const float2* rowa = frame + ra * HP;
+  const float2* rowb = rowa + HP;
+#pragma unroll
+  for (int j = 0; j < 16; ++j) {
+    const int kk = g + G * j;
+    float2 ya, yb;
+    if (j < 8 || (j == 8 && g == 0)) {
+      ya = rowa[kk];
+      yb = rowb[kk];
+    } else {
+      ya = rowa[N - kk];
+      yb = rowb[N - kk];
+      ya.y = -ya.y;
+      yb.y = -yb.y;
+    }
+    v[j] = make_float2(ya.x - yb.y, ya.y + yb.x);
+  }
+  fft_inv<N>(v, g, scr, tw, gmask);
+}
+
+// Column u (u == 0: columns 0 and N/2 packed as re/im) of rows [base, base+rows).
+template <int N>
+__device__ __forceinline__ void load_column(const float2* frame, int u, int base, int rows, int g,
                                             float2 (&v)[16]) {
   constexpr int G = FftShape<N>::G;
   constexpr int HP = frame_pitch(N);
@@ -177,21 +194,21 @@ __device__ __forceinline__ void load_column(const float2* frame, int u, int rows
   for (int mm = 0; mm < 16; ++mm) {
     const int r = g + G * mm;
     if (r < rows) {
-      if (u == 0) v[mm] = make_float2(frame[r * HP].x, frame[r * HP + N / 2].x);
-      else v[mm] = frame[r * HP + u];
+      const float2* row = frame + (base + r) * HP;
+      v[mm] = (u == 0) ? make_float2(row[0].x, row[N / 2].x) : row[u];
     } else {
       v[mm] = make_float2(0.f, 0.f);
     }
   }
 }
 
-// Store an inverse-transformed column to rows [base, base + even(rows)).
+// Inverse-transformed column u to rows [base, base + even(rows)).
 template <int N>
 __device__ __forceinline__ void store_column(float2* frame, int u, int base, int rows, int g,
                                              const float2 (&v)[16]) {
   constexpr int G = FftShape<N>::G;
   constexpr int HP = frame_pitch(N);
-  const int rows_e = (rows + 1) & ~1;
+  const int rows_e = even_up(rows);
 #pragma unroll
   for (int mm = 0; mm < 16; ++mm) {
     const int r = g + G * mm;
@@ -207,166 +224,276 @@ __device__ __forceinline__ void store_column(float2* frame, int u, int base, int
   }
 }
 
-// Spectrum of column unit u: two columns for u == 0.
+// Column spectrum of a real-row-transformed operand.  u != 0: a[] is the
+// spectrum of column u.  u == 0: the packed transform of columns 0 and N/2 is
+// split into a[] (column 0) and b[] (column N/2).
 template <int N>
-struct ColSpec {
-  float2 a[16];  // column u (u == 0: column 0)
-  float2 b[16];  // u == 0: column N/2
-};
+__device__ __forceinline__ void column_spectrum(const float2* frame, int u, int base, int rows,
+                                                int g, float2* scr, const float2* tw,
+                                                unsigned gmask, float2 (&a)[16], float2 (&b)[16]) {
+  load_column<N>(frame, u, base, rows, g, a);
+  fft_fwd<N>(a, g, scr, tw, gmask);
+  if (u == 0) {
+    float2 p[16];
+    hermitian_partner<N>(a, p, g, gmask);
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      const float2 v = a[j];
+      a[j] = make_float2(0.5f * (v.x + p[j].x), 0.5f * (v.y - p[j].y));
+      b[j] = make_float2(0.5f * (v.y + p[j].y), 0.5f * (p[j].x - v.x));
+    }
+  }
+}
 
-// Pointwise product of an operand column spectrum with a cached spectrum,
-// packed for one inverse transform; scale = 1/N^2.
+template <int N>
+__device__ __forceinline__ void store_spectrum(float2* __restrict__ dst, int u, int g,
+                                               const float2 (&a)[16], const float2 (&b)[16]) {
+  constexpr int G = FftShape<N>::G;
+  float2* c0 = dst + (long long)u * N;
+#pragma unroll
+  for (int j = 0; j < 16; ++j) c0[g + G * j] = a[j];
+  if (u == 0) {
+    float2* cN = dst + (long long)(N / 2) * N;
+#pragma unroll
+    for (int j = 0; j < 16; ++j) cN[g + G * j] = b[j];
+  }
+}
+
+// Product of the column spectrum (a, b) with a cached spectrum, packed for
+// one inverse transform (u == 0: column 0 product + i * column N/2 product).
 template <int N, bool CONJ>
-__device__ __forceinline__ void column_product(const ColSpec<N>& s, const float2* __restrict__ bh,
-                                               int u, int g, float scale, float2 (&out)[16]) {
+__device__ __forceinline__ void column_product(const float2 (&a)[16], const float2 (&b)[16],
+                                               const float2* __restrict__ bh, int u, int g,
+                                               float scale, float2 (&out)[16]) {
   constexpr int G = FftShape<N>::G;
   const float2* c0 = bh + (long long)u * N;
   if (u != 0) {
 #pragma unroll
     for (int j = 0; j < 16; ++j) {
-      const float2 b = __ldg(c0 + g + G * j);
-      out[j] = cscale(CONJ ? cmulc(s.a[j], b) : cmul(s.a[j], b), scale);
+      const float2 s = __ldg(c0 + g + G * j);
+      out[j] = cscale(CONJ ? cmulc(a[j], s) : cmul(a[j], s), scale);
     }
   } else {
     const float2* cN = bh + (long long)(N / 2) * N;
 #pragma unroll
     for (int j = 0; j < 16; ++j) {
-      const float2 b0 = __ldg(c0 + g + G * j);
-      const float2 bN = __ldg(cN + g + G * j);
-      const float2 p0 = CONJ ? cmulc(s.a[j], b0) : cmul(s.a[j], b0);
-      const float2 pN = CONJ ? cmulc(s.b[j], bN) : cmul(s.b[j], bN);
+      const float2 s0 = __ldg(c0 + g + G * j);
+      const float2 sN = __ldg(cN + g + G * j);
+      const float2 p0 = CONJ ? cmulc(a[j], s0) : cmul(a[j], s0);
+      const float2 pN = CONJ ? cmulc(b[j], sN) : cmul(b[j], sN);
       out[j] = make_float2((p0.x - pN.y) * scale, (p0.y + pN.x) * scale);
     }
   }
 }
 
+// OP_FWD_BOTH, column unit 0: columns 0 and N/2 of both operands are real.
+// Column 0 of the image and column 0 of the PSFs share one complex transform
+// (then column N/2 of both); the two products are packed as
+// col0 + i*colN for one inverse transform.
 template <int N>
-__device__ __forceinline__ void store_spectrum(float2* __restrict__ dst, const ColSpec<N>& s, int u,
-                                               int g) {
+__device__ __forceinline__ void fwd_both_dc(float2* frame, int rowsA, int baseB, int rowsB, int E0,
+                                            int g, float2* scr, const float2* tw, unsigned gmask,
+                                            float scale, float2* a_out, float2* b_out) {
   constexpr int G = FftShape<N>::G;
-  float2* c0 = dst + (long long)u * N;
+  constexpr int HP = frame_pitch(N);
+  float2 prod[16];
+#pragma unroll 1
+  for (int half = 0; half < 2; ++half) {
+    const int col = half ? N / 2 : 0;
+    float2 v[16];
 #pragma unroll
-  for (int j = 0; j < 16; ++j) c0[g + G * j] = s.a[j];
-  if (u == 0) {
-    float2* cN = dst + (long long)(N / 2) * N;
-#pragma unroll
-    for (int j = 0; j < 16; ++j) cN[g + G * j] = s.b[j];
-  }
-}
-
-template <int N>
-__device__ __forceinline__ void column_spectrum(const float2* frame, int u, int rows, int g,
-                                                float2* scr, const float2* tw, unsigned gmask,
-                                                ColSpec<N>& s) {
-  load_column<N>(frame, u, rows, g, s.a);
-  fft_fwd<N>(s.a, g, scr, tw, gmask);
-  if (u == 0) {
-    // Columns 0 and N/2 are real: split X = A + iB into A and B.
+    for (int mm = 0; mm < 16; ++mm) {
+      const int r = g + G * mm;
+      v[mm] = make_float2(r < rowsA ? frame[r * HP + col].x : 0.f,
+                          r < rowsB ? frame[(baseB + r) * HP + col].x : 0.f);
+    }
+    fft_fwd<N>(v, g, scr, tw, gmask);
     float2 p[16];
-    hermitian_partner<N>(s.a, p, g, gmask);
+    hermitian_partner<N>(v, p, g, gmask);
 #pragma unroll
     for (int j = 0; j < 16; ++j) {
-      const float2 v = s.a[j];
-      s.a[j] = make_float2(0.5f * (v.x + p[j].x), 0.5f * (v.y - p[j].y));
-      s.b[j] = make_float2(0.5f * (v.y + p[j].y), 0.5f * (p[j].x - v.x));
+      const float2 sa = make_float2(0.5f * (v[j].x + p[j].x), 0.5f * (v[j].y - p[j].y));
+      const float2 sb = make_float2(0.5f * (v[j].y + p[j].y), 0.5f * (p[j].x - v[j].x));
+      if (a_out) a_out[(long long)col * N + g + G * j] = sa;
+      if (b_out) b_out[(long long)col * N + g + G * j] = sb;
+      const float2 pj = cscale(cmul(sa, sb), scale);
+      prod[j] = half ? make_float2(prod[j].x - pj.y, prod[j].y + pj.x) : pj;
     }
   }
+  fft_inv<N>(prod, g, scr, tw, gmask);
+  store_column<N>(frame, 0, 0, E0, g, prod);
 }
 
 template <int N, int OP>
-__global__ void __launch_bounds__(256) eff_kernel(Params P) {
+__global__ void __launch_bounds__(max_threads(N)) eff_kernel(Params P) {
   constexpr int G = FftShape<N>::G;
-  constexpr int HP = frame_pitch(N);
+  constexpr int A = opnd_a(OP);
   extern __shared__ __align__(16) float2 smem[];
-  float2* tw = smem;                 // N entries
-  float2* frame = smem + N;          // rows * HP (rows set by the host)
+  float2* tw = smem;         // N entries
+  float2* frame = smem + N;  // frame_rows(P, OP) * (N/2+1)
   const int tid = threadIdx.x;
   const int NG = blockDim.x / G;
   const int gid = tid / G, g = tid % G;
   const unsigned gmask = group_mask<N>(tid & 31);
 
-  const int k = blockIdx.x;
-  const int m = k / P.csf1, n = k - (k / P.csf1) * P.csf1;
+  Patch T;
+  T.k = blockIdx.x;
+  T.m = T.k / P.csf1;
+  T.n = T.k - T.m * P.csf1;
   const long long b = blockIdx.y;
-  const float* x = P.x ? P.x + b * P.x_bs : nullptr;
-  const float* f = P.f ? P.f + b * P.f_bs : nullptr;
-  const float* y = P.y ? P.y + b * P.y_bs : nullptr;
+  T.x = P.x ? P.x + b * P.x_bs : nullptr;
+  T.f = P.f ? P.f + b * P.f_bs : nullptr;
+  T.y = P.y ? P.y + b * P.y_bs : nullptr;
+  T.y_obs = P.y_obs ? P.y_obs + b * P.y_bs : nullptr;
   const long long spec_patch = (long long)(N / 2 + 1) * N;
-  const float2* b0 = P.b0 ? P.b0 + b * P.spec_bs + k * spec_patch : nullptr;
-  const float2* b1 = P.b1 ? P.b1 + b * P.spec_bs + k * spec_patch : nullptr;
-  float2* a_out = P.a_out ? P.a_out + b * P.spec_bs + k * spec_patch : nullptr;
+  const long long spec_off = b * P.spec_bs + T.k * spec_patch;
+  const float2* b0 = P.b0 ? P.b0 + spec_off : nullptr;
+  const float2* b1 = P.b1 ? P.b1 + spec_off : nullptr;
+  float2* a_out = P.a_out ? P.a_out + spec_off : nullptr;
+  float2* b_out = P.b_out ? P.b_out + spec_off : nullptr;
 
-  // Frame rows in use (same formula as the host's shared-memory sizing).
-  int rows_alloc;
-  if constexpr (OP == OP_SPEC_IMAGE || OP == OP_SPEC_PSF) rows_alloc = (operand_rows<OP>(P) + 1) & ~1;
-  else if constexpr (OP == OP_FWD_IMAGE || OP == OP_FWD_PSF) rows_alloc = (P.E0 + 1) & ~1;
-  else {
-    const int r0 = P.out0 ? ((P.sw0 + 1) & ~1) : 0;
-    const int r1 = P.out1 ? ((P.sf0 + 1) & ~1) : 0;
-    rows_alloc = max((P.E0 + 1) & ~1, r0 + r1);
-  }
-  float2* scr = frame + rows_alloc * HP + gid * FftShape<N>::SCR;
+  const int rowsA = opnd_rows(P, A);
+  const int baseB = even_up(rowsA);
+  float2* scr = frame + frame_rows(P, OP) * frame_pitch(N) + gid * FftShape<N>::SCR;
 
   for (int i = tid; i < N; i += blockDim.x) tw[i] = __ldg(P.tw + i);
+
+  // Loss of the residual: this CTA's contiguous share of the pixels.
+  if constexpr (OP == OP_ADJ) {
+    if (P.loss && T.y_obs) {
+      const long long npx = (long long)P.sy0 * P.sy1;
+      const long long chunk = (npx + gridDim.x - 1) / gridDim.x;
+      const long long p0 = T.k * chunk;
+      const long long p1 = min(npx, p0 + chunk);
+      float acc = 0.f;
+      for (long long p = p0 + tid; p < p1; p += blockDim.x) {
+        const float r = __ldg(T.y + p) - __ldg(T.y_obs + p);
+        acc = fmaf(r, r, acc);
+      }
+      double d = acc;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+      if ((tid & 31) == 0) atomicAdd(P.loss + b, 0.5 * d);
+    }
+  }
   __syncthreads();
 
-  row_r2c<N, OP>(P, x, f, y, m, n, k, frame, scr, tw, gid, NG, g, gmask);
+  // Phase 1: row transforms of operand A (and B).
+  {
+    const int nA = (rowsA + 1) >> 1;
+    const int nB = has_b(OP) ? (P.sf0 + 1) >> 1 : 0;
+    for (int u = gid; u < nA + nB; u += NG) {
+      if (u < nA) r2c_unit<N, A>(P, T, 2 * u, frame, 0, scr, tw, g, gmask);
+      else r2c_unit<N, OPND_PSF>(P, T, 2 * (u - nA), frame, baseB, scr, tw, g, gmask);
+    }
+  }
   __syncthreads();
 
-  const int rowsA = operand_rows<OP>(P);
+  // Phase 2: column transforms, products, inverse column transforms.
   const float scale = 1.f / (float(N) * float(N));
   for (int u = gid; u < N / 2; u += NG) {
-    ColSpec<N> s;
-    column_spectrum<N>(frame, u, rowsA, g, scr, tw, gmask, s);
+    if constexpr (OP == OP_FWD_BOTH) {
+      if (u == 0) {
+        fwd_both_dc<N>(frame, rowsA, baseB, P.sf0, P.E0, g, scr, tw, gmask, scale, a_out, b_out);
+        continue;
+      }
+    }
+    float2 a[16], ab[16];
+    column_spectrum<N>(frame, u, 0, rowsA, g, scr, tw, gmask, a, ab);
     if constexpr (OP == OP_SPEC_IMAGE || OP == OP_SPEC_PSF) {
-      store_spectrum<N>(a_out, s, u, g);
+      store_spectrum<N>(a_out, u, g, a, ab);
     } else if constexpr (OP == OP_FWD_IMAGE || OP == OP_FWD_PSF) {
-      if (a_out) store_spectrum<N>(a_out, s, u, g);
+      if (a_out) store_spectrum<N>(a_out, u, g, a, ab);
       float2 pr[16];
-      column_product<N, false>(s, b0, u, g, scale, pr);
+      column_product<N, false>(a, ab, b0, u, g, scale, pr);
       fft_inv<N>(pr, g, scr, tw, gmask);
       store_column<N>(frame, u, 0, P.E0, g, pr);
+    } else if constexpr (OP == OP_FWD_BOTH) {
+      // u != 0 here
+      if (a_out) store_spectrum<N>(a_out, u, g, a, ab);
+      float2 s[16];
+      load_column<N>(frame, u, baseB, P.sf0, g, s);
+      fft_fwd<N>(s, g, scr, tw, gmask);
+      if (b_out) store_spectrum<N>(b_out, u, g, s, s);
+#pragma unroll
+      for (int j = 0; j < 16; ++j) a[j] = cscale(cmul(a[j], s[j]), scale);
+      fft_inv<N>(a, g, scr, tw, gmask);
+      store_column<N>(frame, u, 0, P.E0, g, a);
     } else {
-      if (P.out0) {
+      // adjoints: output 0 = image (conj F-hat, rows sw0), 1 = PSF (conj X-hat, rows sf0)
+#pragma unroll 1
+      for (int o = 0; o < 2; ++o) {
+        if (o == 0 ? !P.out0 : !P.out1) continue;
         float2 pr[16];
-        column_product<N, true>(s, b0, u, g, scale, pr);
+        column_product<N, true>(a, ab, o == 0 ? b0 : b1, u, g, scale, pr);
         fft_inv<N>(pr, g, scr, tw, gmask);
-        store_column<N>(frame, u, 0, P.sw0, g, pr);
-      }
-      if (P.out1) {
-        float2 pr[16];
-        column_product<N, true>(s, b1, u, g, scale, pr);
-        fft_inv<N>(pr, g, scr, tw, gmask);
-        store_column<N>(frame, u, P.out0 ? ((P.sw0 + 1) & ~1) : 0, P.sf0, g, pr);
+        const int base = (o == 1 && P.out0) ? even_up(P.sw0) : 0;
+        store_column<N>(frame, u, base, o == 0 ? P.sw0 : P.sf0, g, pr);
       }
     }
   }
   if constexpr (OP == OP_SPEC_IMAGE || OP == OP_SPEC_PSF) return;
   __syncthreads();
 
-  if constexpr (OP == OP_FWD_IMAGE || OP == OP_FWD_PSF) {
+  // Phase 3: inverse row transforms and epilogues.
+  if constexpr (OP == OP_FWD_IMAGE || OP == OP_FWD_PSF || OP == OP_FWD_BOTH) {
     float* out = P.out0 + b * P.out0_bs;
-    const int i0 = m * P.hop0 - P.off0, j0 = n * P.hop1 - P.off1;
-    row_c2r<N>(frame, 0, P.E0, P.E1, scr, tw, gid, NG, g, gmask, [&](int r, int c, float val) {
-      const int i = i0 + r, j = j0 + c;
-      if (i >= 0 && j >= 0 && i < P.sy0 && j < P.sy1) atomicAdd(out + (long long)i * P.sy1 + j, val);
-    });
-  } else if constexpr (OP == OP_ADJ) {
-    if (P.out0) {
-      float* out = P.out0 + b * P.out0_bs;
-      const float2* w0 = P.win0 + m * P.sw0;
-      const float2* w1 = P.win1 + n * P.sw1;
-      const int i0 = m * P.hop0, j0 = n * P.hop1;
-      row_c2r<N>(frame, 0, P.sw0, P.sw1, scr, tw, gid, NG, g, gmask, [&](int r, int c, float val) {
-        const int i = i0 + r, j = j0 + c;
-        if (i < P.sx0 && j < P.sx1)
-          atomicAdd(out + (long long)i * P.sx1 + j, val * window_weight(__ldg(w0 + r), __ldg(w1 + c)));
-      });
+    const int i0 = T.m * P.hop0 - P.off0, j0 = T.n * P.hop1 - P.off1;
+    const int nu = (P.E0 + 1) >> 1;
+    for (int u = gid; u < nu; u += NG) {
+      float2 v[16];
+      c2r_unit<N>(frame, 2 * u, v, scr, tw, g, gmask);
+      const int ia = i0 + 2 * u;
+      const bool rb = 2 * u + 1 < P.E0;
+#pragma unroll
+      for (int mm = 0; mm < 16; ++mm) {
+        const int c = g + G * mm, j = j0 + c;
+        if (c < P.E1 && j >= 0 && j < P.sy1) {
+          if (ia >= 0 && ia < P.sy0) atomicAdd(out + (long long)ia * P.sy1 + j, v[mm].x);
+          if (rb && ia + 1 >= 0 && ia + 1 < P.sy0) atomicAdd(out + (long long)(ia + 1) * P.sy1 + j, v[mm].y);
+        }
+      }
     }
-    if (P.out1) {
-      float* out = P.out1 + b * P.out1_bs + (long long)k * P.sf0 * P.sf1;
-      row_c2r<N>(frame, P.out0 ? ((P.sw0 + 1) & ~1) : 0, P.sf0, P.sf1, scr, tw, gid, NG, g, gmask,
-                 [&](int r, int c, float val) { out[r * P.sf1 + c] = val; });
+  } else if constexpr (OP == OP_ADJ) {
+    const int n0 = P.out0 ? (P.sw0 + 1) >> 1 : 0;
+    const int n1 = P.out1 ? (P.sf0 + 1) >> 1 : 0;
+    const int base1 = P.out0 ? even_up(P.sw0) : 0;
+    for (int u = gid; u < n0 + n1; u += NG) {
+      float2 v[16];
+      if (u < n0) {
+        // image gradient: window, overlap-add into gx
+        c2r_unit<N>(frame, 2 * u, v, scr, tw, g, gmask);
+        float* out = P.out0 + b * P.out0_bs;
+        const int r = 2 * u;
+        const int i = T.m * P.hop0 + r;
+        const float2 wa = __ldg(P.win0 + T.m * P.sw0 + r);
+        const float2 wb = (r + 1 < P.sw0) ? __ldg(P.win0 + T.m * P.sw0 + r + 1) : make_float2(0.f, 0.f);
+        const bool rb = r + 1 < P.sw0;
+#pragma unroll
+        for (int mm = 0; mm < 16; ++mm) {
+          const int c = g + G * mm, j = T.n * P.hop1 + c;
+          if (c < P.sw1 && j < P.sx1) {
+            const float2 wc = __ldg(P.win1 + T.n * P.sw1 + c);
+            if (i < P.sx0) atomicAdd(out + (long long)i * P.sx1 + j, v[mm].x * window_weight(wa, wc));
+            if (rb && i + 1 < P.sx0)
+              atomicAdd(out + (long long)(i + 1) * P.sx1 + j, v[mm].y * window_weight(wb, wc));
+          }
+        }
+      } else {
+        // PSF gradient: crop to sf
+        const int r = 2 * (u - n0);
+        c2r_unit<N>(frame, base1 + r, v, scr, tw, g, gmask);
+        float* out = P.out1 + b * P.out1_bs + (long long)T.k * P.sf0 * P.sf1;
+        const bool rb = r + 1 < P.sf0;
+#pragma unroll
+        for (int mm = 0; mm < 16; ++mm) {
+          const int c = g + G * mm;
+          if (c < P.sf1) {
+            out[r * P.sf1 + c] = v[mm].x;
+            if (rb) out[(r + 1) * P.sf1 + c] = v[mm].y;
+          }
+        }
+      }
     }
   }
 }

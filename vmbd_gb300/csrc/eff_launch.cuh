@@ -5,22 +5,12 @@
 
 namespace eff {
 
-// Shared-memory bytes of one CTA (same row count as eff_kernel computes).
+// Shared-memory bytes of one CTA: twiddles + frame + per-group exchange scratch.
 inline size_t smem_bytes(int N, int op, const Params& P, int threads) {
   const int G = N / 16;
-  const int HP = N / 2 + 1;
   const int scr = 16 * (G + 1) + 8;
-  int rows;
-  auto even = [](int v) { return (v + 1) & ~1; };
-  if (op == OP_SPEC_IMAGE) rows = even(P.sw0);
-  else if (op == OP_SPEC_PSF) rows = even(P.sf0);
-  else if (op == OP_FWD_IMAGE || op == OP_FWD_PSF) rows = even(P.E0);
-  else {
-    const int r0 = P.out0 ? even(P.sw0) : 0;
-    const int r1 = P.out1 ? even(P.sf0) : 0;
-    rows = even(P.E0) > r0 + r1 ? even(P.E0) : r0 + r1;
-  }
-  return sizeof(float2) * ((size_t)N + (size_t)rows * HP + (size_t)(threads / G) * scr);
+  return sizeof(float2) * ((size_t)N + (size_t)frame_rows(P, op) * frame_pitch(N) +
+                           (size_t)(threads / G) * scr);
 }
 
 template <int N, int OP>
@@ -29,10 +19,10 @@ cudaError_t launch_one(const Params& P, int K, int batch, int threads, size_t sm
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
-  if (dev < 64 && attr_bytes[dev].load() < (int)smem) {
+  if (dev >= 64 || attr_bytes[dev].load() < (int)smem) {
     e = cudaFuncSetAttribute(eff_kernel<N, OP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    attr_bytes[dev].store((int)smem);
+    if (dev < 64) attr_bytes[dev].store((int)smem);
   }
   eff_kernel<N, OP><<<dim3(K, batch), threads, smem, st>>>(P);
   return cudaGetLastError();
@@ -45,6 +35,7 @@ cudaError_t launch_n(int op, const Params& P, int K, int batch, int threads, siz
     case OP_SPEC_PSF: return launch_one<N, OP_SPEC_PSF>(P, K, batch, threads, smem, st);
     case OP_FWD_IMAGE: return launch_one<N, OP_FWD_IMAGE>(P, K, batch, threads, smem, st);
     case OP_FWD_PSF: return launch_one<N, OP_FWD_PSF>(P, K, batch, threads, smem, st);
+    case OP_FWD_BOTH: return launch_one<N, OP_FWD_BOTH>(P, K, batch, threads, smem, st);
     case OP_ADJ: return launch_one<N, OP_ADJ>(P, K, batch, threads, smem, st);
     default: return cudaErrorInvalidValue;
   }

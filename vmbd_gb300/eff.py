@@ -145,8 +145,62 @@ class EffPlan:
                                             b or 1, _stream(self.device)))
         return out
 
+    def forward_both(self, x, f, out=None, xhat_out=None, fhat_out=None):
+        """y = EFF(x, f) from raw image and PSFs in one kernel; optionally
+        leaves both spectra behind for a later ``adjoint``."""
+        x, b = self._check(x, self.sx, "x")
+        f, bf = self._check(f, (self.K,) + self.sf, "f")
+        if bf != b:
+            raise IOError("Size missmatch: x and f batch dims differ")
+        for s_, n in ((xhat_out, "xhat_out"), (fhat_out, "fhat_out")):
+            if s_ is not None:
+                self._check_spec(s_, b, n)
+        if out is None:
+            out = torch.empty(((b,) if b else ()) + self.sy, dtype=torch.float32, device=self.device)
+        _lib.check(self.lib.eff_forward_both(self._h, _ptr(x), _ptr(f), _ptr(out), _ptr(xhat_out),
+                                             _ptr(fhat_out), b or 1, _stream(self.device)))
+        return out
+
+    def workspace(self, batch=None) -> torch.Tensor:
+        """Device workspace of ``loss_grad`` (cached per batch size)."""
+        key = batch or 1
+        if not hasattr(self, "_ws"):
+            self._ws = {}
+        if key not in self._ws:
+            n = self.lib.eff_loss_grad_workspace_bytes(self._h, key)
+            self._ws[key] = torch.empty(n, dtype=torch.uint8, device=self.device)
+        return self._ws[key]
+
+    def loss_grad(self, x, f, y_obs, want_image=True, want_psf=True, loss=None, gx=None, gf=None):
+        """``0.5*||EFF(x, f) - y_obs||^2`` and its gradients w.r.t. x and f:
+        two kernels (fused forward, fused adjoints of the residual).  Returns
+        ``(loss [float64], gx, gf)``."""
+        x, b = self._check(x, self.sx, "x")
+        f, _ = self._check(f, (self.K,) + self.sf, "f")
+        y_obs, _ = self._check(y_obs, self.sy, "y_obs")
+        lead = (b,) if b else ()
+        if loss is None:
+            loss = torch.empty(lead, dtype=torch.float64, device=self.device)
+        if want_image and gx is None:
+            gx = torch.empty(lead + self.sx, dtype=torch.float32, device=self.device)
+        if want_psf and gf is None:
+            gf = torch.empty(lead + (self.K,) + self.sf, dtype=torch.float32, device=self.device)
+        gx = gx if want_image else None
+        gf = gf if want_psf else None
+        ws = self.workspace(b)
+        _lib.check(self.lib.eff_loss_grad(self._h, _ptr(x), _ptr(f), _ptr(y_obs), _ptr(loss), _ptr(gx),
+                                          _ptr(gf), _ptr(ws), ws.numel(), b or 1, _stream(self.device)))
+        return loss, gx, gf
+
+    def adjoint_residual(self, y, y_obs, fhat=None, xhat=None, want_image=True, want_psf=True,
+                         loss=None, gx=None, gf=None, adjoint="exact"):
+        """``adjoint(y - y_obs)`` without forming the residual; also returns
+        ``0.5*||y - y_obs||^2`` (float64).  Returns ``(loss, gx, gf)``."""
+        return self.adjoint(y, fhat, xhat, want_image, want_psf, adjoint, gx, gf, y_obs=y_obs,
+                            loss=loss)
+
     def adjoint(self, y, fhat=None, xhat=None, want_image=True, want_psf=True,
-                adjoint="exact", gx=None, gf=None):
+                adjoint="exact", gx=None, gf=None, y_obs=None, loss=None):
         """F.cnvtp(y) and/or X.cnvtp(y) from one transform of y.
 
         Returns ``(gx, gf)``; an output that is not wanted is None.
@@ -175,10 +229,19 @@ class EffPlan:
         else:
             gf = None
         mode = _lib.ADJ_EXACT if adjoint == "exact" else _lib.ADJ_REFERENCE
-        _lib.check(self.lib.eff_adjoint(self._h, _ptr(y), _ptr(fhat if want_image else None),
-                                        _ptr(xhat if want_psf else None), _ptr(gx), _ptr(gf), mode,
-                                        b or 1, _stream(self.device)))
-        return gx, gf
+        if y_obs is None:
+            _lib.check(self.lib.eff_adjoint(self._h, _ptr(y), _ptr(fhat if want_image else None),
+                                            _ptr(xhat if want_psf else None), _ptr(gx), _ptr(gf), mode,
+                                            b or 1, _stream(self.device)))
+            return gx, gf
+        y_obs, _ = self._check(y_obs, self.sy, "y_obs")
+        if loss is None:
+            loss = torch.empty(lead, dtype=torch.float64, device=self.device)
+        _lib.check(self.lib.eff_adjoint_residual(self._h, _ptr(y), _ptr(y_obs),
+                                                 _ptr(fhat if want_image else None),
+                                                 _ptr(xhat if want_psf else None), _ptr(gx), _ptr(gf),
+                                                 _ptr(loss), mode, b or 1, _stream(self.device)))
+        return loss, gx, gf
 
 
 def project_psf(f: torch.Tensor, mode: str = "simplex") -> torch.Tensor:

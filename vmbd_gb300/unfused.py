@@ -53,10 +53,11 @@ class UnfusedEff:
         je = torch.arange(self.csf[1], device=dev)[:, None] * self.hop[1] + torch.arange(E[1], device=dev)
         self.ie, self.je = ie, je
 
-    def _chop(self, img, ii, jj, pad_to):
-        """[H, W] -> [K, len(ii), len(jj)] gather (zero outside the image)."""
-        H = max(int(ii.max()) + 1, img.shape[0])
-        W = max(int(jj.max()) + 1, img.shape[1])
+    def _chop(self, img, ii, jj, ext):
+        """[H, W] -> [K, len(ii), len(jj)] gather (zero outside the image);
+        ``ext`` is the patch extent the indices cover."""
+        H = max(self.hop[0] * (self.csf[0] - 1) + ext[0], img.shape[0])
+        W = max(self.hop[1] * (self.csf[1] - 1) + ext[1], img.shape[1])
         p = F.pad(img, (0, W - img.shape[1], 0, H - img.shape[0]))
         pt = p[ii[:, None, :, None], jj[None, :, None, :]]  # [cm, cn, a, b]
         return pt.reshape(self.K, ii.shape[1], jj.shape[1])
@@ -76,7 +77,7 @@ class UnfusedEff:
 
     def image_spectrum(self, x):
         N = self.N
-        u = self._chop(x, self.ii, self.jj, N) * self.ws
+        u = self._chop(x, self.ii, self.jj, self.sw) * self.ws
         u = F.pad(u, (0, N - self.sw[1], 0, N - self.sw[0]))
         return torch.fft.fft2(u.to(torch.complex64))
 
@@ -99,7 +100,7 @@ class UnfusedEff:
         h = min(self.sy[0], self.full[0] - o[0])
         w = min(self.sy[1], self.full[1] - o[1])
         emb[o[0]:o[0] + h, o[1]:o[1] + w] = y[:h, :w]
-        fr = self._chop(emb, self.ie, self.je, N)
+        fr = self._chop(emb, self.ie, self.je, self.E)
         fr = F.pad(fr, (0, N - self.E[1], 0, N - self.E[0]))
         yh = torch.fft.fft2(fr.to(torch.complex64))
         zx = torch.fft.ifft2(yh * fhat.conj()).real[:, :self.sw[0], :self.sw[1]] * self.ws
