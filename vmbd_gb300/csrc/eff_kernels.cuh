@@ -130,23 +130,29 @@ __device__ __forceinline__ float operand(const Params& P, const Patch& T, int r,
   }
 }
 
-// R2C of one pair of operand rows (ra, ra+1) into frame rows base+ra, base+ra+1.
+// Operand rows (ra, ra+1) packed as re/im, layout A.
 template <int N, int KIND>
-__device__ __forceinline__ void r2c_unit(const Params& P, const Patch& T, int ra, float2* frame,
-                                         int base, float2* scr, const float2* tw, int g,
-                                         unsigned gmask) {
+__device__ __forceinline__ void load_rows(const Params& P, const Patch& T, int ra, int g,
+                                          float2 (&v)[16]) {
   constexpr int G = FftShape<N>::G;
-  constexpr int HP = frame_pitch(N);
-  float2 v[16];
 #pragma unroll
   for (int mm = 0; mm < 16; ++mm) {
     const int c = g + G * mm;
     v[mm] = make_float2(operand<KIND>(P, T, ra, c), operand<KIND>(P, T, ra + 1, c));
   }
+}
+
+// R2C of one pair of rows already in v (layout A) into frame rows
+// base+ra, base+ra+1.
+template <int N>
+__device__ __forceinline__ void r2c_store(float2 (&v)[16], float2* frame, int row, float2* scr,
+                                          const float2* tw, int g, unsigned gmask) {
+  constexpr int G = FftShape<N>::G;
+  constexpr int HP = frame_pitch(N);
   fft_fwd<N>(v, g, scr, tw, gmask);
   float2 p[16];
   hermitian_partner<N>(v, p, g, gmask);
-  float2* rowa = frame + (base + ra) * HP;
+  float2* rowa = frame + row * HP;
   float2* rowb = rowa + HP;
 #pragma unroll
   for (int j = 0; j <= 8; ++j) {
@@ -301,19 +307,35 @@ __device__ __forceinline__ void fwd_both_dc(float2* frame, int rowsA, int baseB,
   for (int half = 0; half < 2; ++half) {
     const int col = half ? N / 2 : 0;
     float2 v[16];
+    float amax = 0.f, bmax = 0.f;
 #pragma unroll
     for (int mm = 0; mm < 16; ++mm) {
       const int r = g + G * mm;
       v[mm] = make_float2(r < rowsA ? frame[r * HP + col].x : 0.f,
                           r < rowsB ? frame[(baseB + r) * HP + col].x : 0.f);
+      amax = fmaxf(amax, fabsf(v[mm].x));
+      bmax = fmaxf(bmax, fabsf(v[mm].y));
     }
+    // The two columns can differ in magnitude by orders (image row sums vs
+    // PSF row sums); one complex transform rounds both relative to the
+    // larger, so bring the PSF column to the image's scale by an exact power
+    // of two first and undo it after the split.
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) {
+      amax = fmaxf(amax, __shfl_xor_sync(gmask, amax, o, G));
+      bmax = fmaxf(bmax, __shfl_xor_sync(gmask, bmax, o, G));
+    }
+    const int e = (amax > 0.f && bmax > 0.f) ? ilogbf(amax) - ilogbf(bmax) : 0;
+    const float up = ldexpf(1.f, e), down = ldexpf(0.5f, -e);  // down folds the split's 1/2
+#pragma unroll
+    for (int mm = 0; mm < 16; ++mm) v[mm].y *= up;
     fft_fwd<N>(v, g, scr, tw, gmask);
     float2 p[16];
     hermitian_partner<N>(v, p, g, gmask);
 #pragma unroll
     for (int j = 0; j < 16; ++j) {
       const float2 sa = make_float2(0.5f * (v[j].x + p[j].x), 0.5f * (v[j].y - p[j].y));
-      const float2 sb = make_float2(0.5f * (v[j].y + p[j].y), 0.5f * (p[j].x - v[j].x));
+      const float2 sb = make_float2(down * (v[j].y + p[j].y), down * (p[j].x - v[j].x));
       if (a_out) a_out[(long long)col * N + g + G * j] = sa;
       if (b_out) b_out[(long long)col * N + g + G * j] = sb;
       const float2 pj = cscale(cmul(sa, sb), scale);
@@ -383,8 +405,16 @@ __global__ void __launch_bounds__(max_threads(N)) eff_kernel(Params P) {
     const int nA = (rowsA + 1) >> 1;
     const int nB = has_b(OP) ? (P.sf0 + 1) >> 1 : 0;
     for (int u = gid; u < nA + nB; u += NG) {
-      if (u < nA) r2c_unit<N, A>(P, T, 2 * u, frame, 0, scr, tw, g, gmask);
-      else r2c_unit<N, OPND_PSF>(P, T, 2 * (u - nA), frame, baseB, scr, tw, g, gmask);
+      float2 v[16];
+      int row;
+      if (u < nA) {
+        load_rows<N, A>(P, T, 2 * u, g, v);
+        row = 2 * u;
+      } else {
+        load_rows<N, OPND_PSF>(P, T, 2 * (u - nA), g, v);
+        row = baseB + 2 * (u - nA);
+      }
+      r2c_store<N>(v, frame, row, scr, tw, g, gmask);
     }
   }
   __syncthreads();
@@ -409,7 +439,8 @@ __global__ void __launch_bounds__(max_threads(N)) eff_kernel(Params P) {
       fft_inv<N>(pr, g, scr, tw, gmask);
       store_column<N>(frame, u, 0, P.E0, g, pr);
     } else if constexpr (OP == OP_FWD_BOTH) {
-      // u != 0 here
+      // u != 0 here: a holds the image column spectrum; transform the PSF
+      // column through the same code and multiply in place
       if (a_out) store_spectrum<N>(a_out, u, g, a, ab);
       float2 s[16];
       load_column<N>(frame, u, baseB, P.sf0, g, s);
@@ -459,16 +490,17 @@ __global__ void __launch_bounds__(max_threads(N)) eff_kernel(Params P) {
     const int n1 = P.out1 ? (P.sf0 + 1) >> 1 : 0;
     const int base1 = P.out0 ? even_up(P.sw0) : 0;
     for (int u = gid; u < n0 + n1; u += NG) {
+      const bool img = u < n0;
+      const int r = img ? 2 * u : 2 * (u - n0);
       float2 v[16];
-      if (u < n0) {
+      c2r_unit<N>(frame, img ? r : base1 + r, v, scr, tw, g, gmask);
+      if (img) {
         // image gradient: window, overlap-add into gx
-        c2r_unit<N>(frame, 2 * u, v, scr, tw, g, gmask);
         float* out = P.out0 + b * P.out0_bs;
-        const int r = 2 * u;
         const int i = T.m * P.hop0 + r;
-        const float2 wa = __ldg(P.win0 + T.m * P.sw0 + r);
-        const float2 wb = (r + 1 < P.sw0) ? __ldg(P.win0 + T.m * P.sw0 + r + 1) : make_float2(0.f, 0.f);
         const bool rb = r + 1 < P.sw0;
+        const float2 wa = __ldg(P.win0 + T.m * P.sw0 + r);
+        const float2 wb = rb ? __ldg(P.win0 + T.m * P.sw0 + r + 1) : make_float2(0.f, 0.f);
 #pragma unroll
         for (int mm = 0; mm < 16; ++mm) {
           const int c = g + G * mm, j = T.n * P.hop1 + c;
@@ -481,8 +513,6 @@ __global__ void __launch_bounds__(max_threads(N)) eff_kernel(Params P) {
         }
       } else {
         // PSF gradient: crop to sf
-        const int r = 2 * (u - n0);
-        c2r_unit<N>(frame, base1 + r, v, scr, tw, g, gmask);
         float* out = P.out1 + b * P.out1_bs + (long long)T.k * P.sf0 * P.sf1;
         const bool rb = r + 1 < P.sf0;
 #pragma unroll
