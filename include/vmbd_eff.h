@@ -121,6 +121,23 @@ int eff_loss_grad(const EffPlan* plan, const float* x, const float* f, const flo
                   double* loss, float* gx, float* gf, void* workspace, size_t workspace_bytes,
                   int batch, void* stream);
 
+/* eff_loss_grad without a workspace argument, for callers that cannot
+ * allocate device memory or pass a workspace: bindings of the reference's
+ * cnvinv_objfun / cnvinv_gradfun interface (olaGPU.py:756-811) hand over only
+ * the data and the outputs, and some host programs reserve all device memory
+ * up front or cannot afford cudaMalloc's implicit synchronisation.  No
+ * counterpart in the reference (it allocates fresh GPU arrays on every call).
+ *
+ * The scratch is a static device array of eff_static_scratch_bytes() bytes
+ * (16 MiB) that every GPU loading the library keeps until the process exits;
+ * larger geometries / batches return EFF_ERR_UNSUPPORTED.  The first call on
+ * a device looks up the array's device address (cudaGetSymbolAddress): make
+ * it before any stream capture.  All calls share the array; calls whose GPU
+ * work overlaps (other streams or threads) race on it.  Allocates nothing. */
+size_t eff_static_scratch_bytes(void);
+int eff_loss_grad_static(const EffPlan* plan, const float* x, const float* f, const float* y_obs,
+                         double* loss, float* gx, float* gf, int batch, void* stream);
+
 /* PSF projections on [K, n] stacks (n = sf0*sf1), in place.
  * EFF_PROJ_CLIP_NORMALIZE: f = max(f, 0) then f /= sum(f) when sum > 1e-6
  *   (L-BFGS-B bounds olaGPU.py:404-411 + normalize gputools.py:1025-1044).

@@ -27,6 +27,7 @@ EXPORTS = (
     "eff_psf_spectrum", "eff_image_spectrum", "eff_forward_image", "eff_forward_psf",
     "eff_adjoint", "eff_project_psf", "eff_basis_project", "eff_last_error",
     "eff_forward_both", "eff_adjoint_residual", "eff_loss_grad_workspace_bytes", "eff_loss_grad",
+    "eff_static_scratch_bytes", "eff_loss_grad_static",
 )
 
 
@@ -77,6 +78,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "eff_adjoint_residual": ([vp, fp, fp, vp, vp, fp, fp, vp, ip, ip, vp], ip),
         "eff_loss_grad_workspace_bytes": ([vp, ip], ctypes.c_size_t),
         "eff_loss_grad": ([vp, fp, fp, fp, vp, fp, fp, vp, ctypes.c_size_t, ip, vp], ip),
+        "eff_static_scratch_bytes": ([], ctypes.c_size_t),
+        "eff_loss_grad_static": ([vp, fp, fp, fp, vp, fp, fp, ip, vp], ip),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)

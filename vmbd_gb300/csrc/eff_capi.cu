@@ -12,6 +12,7 @@
 #include <string>
 #include <vector>
 
+#include "eff_internal.h"
 #include "eff_launch.cuh"
 #include "../../include/vmbd_eff.h"
 
@@ -169,6 +170,8 @@ int loss_grad_impl(const EffPlan* plan, const float* x, const float* f, const fl
 }
 
 }  // namespace
+
+int eff::set_error(int code, const std::string& msg) { return fail(code, msg); }
 
 extern "C" {
 
