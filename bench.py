@@ -46,6 +46,12 @@ WORKLOADS = {
                  sx=(256, 256), csf=(4, 4), sf=(15, 15), sw=(64, 64), hop=(32, 32), kind="gauss"),
 }
 FLUSH_BYTES = 256 << 20
+# Online multi-frame blind deconvolution: 512x512 frames, 25x25 motion PSFs
+# drifting over the sequence on an 8x8 grid, Poisson (peak 1000) + Gaussian
+# (0.005) noise, per frame 10 PG PSF steps (simplex) + 5 multiplicative image
+# steps with edgetaper.  Latent image 536x536 (valid mode), win2winaux patches
+# 120x120 (hop 60), frame 256.
+MFBD = dict(sy=(512, 512), sf=(25, 25), csf=(8, 8), frames=100, n_pg=10, n_mu=5)
 
 
 def peaks():
@@ -318,6 +324,76 @@ def profile_run(args, dev):
     print(json.dumps({"profile": args.workload, "steps": args.steps, "warmup": args.warmup}))
 
 
+def run_mfbd(args, dev, n_timed, with_unfused=True):
+    """Frames/s of the online MFBD loop, one frame per step, graph-captured."""
+    import torch
+    from vmbd_gb300.mfbd import OnlineMFBD, make_sequence
+    from vmbd_gb300.unfused import UnfusedMFBD
+    M = OnlineMFBD(MFBD["sy"], MFBD["sf"], MFBD["csf"], n_pg=MFBD["n_pg"], n_mu=MFBD["n_mu"], device=dev)
+    _, _, ys = make_sequence(M.plan, MFBD["frames"], seed=11)
+    M.init_latent(ys[:20])
+    x0, f0 = M.x.clone(), M.f.clone()
+    flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    nf = MFBD["frames"]
+    with torch.cuda.stream(stream):
+        M.frame(ys[0])
+        torch.cuda.synchronize(dev)
+        M.x.copy_(x0)
+        M.f.copy_(f0)
+        gph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(gph, stream=stream):
+            M.frame(None)
+        torch.cuda.synchronize(dev)
+
+        def timed(replay, total):
+            t = 0.0
+            for i in range(total):
+                flush.fill_(1.0)
+                a = torch.cuda.Event(enable_timing=True)
+                b = torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                replay(i % nf)
+                b.record(stream)
+                torch.cuda.synchronize(dev)
+                if i >= args.warmup:
+                    t += a.elapsed_time(b)
+            return t / (total - args.warmup)
+
+        def ours(i):
+            M.y.copy_(ys[i])
+            gph.replay()
+
+        ms = timed(ours, args.warmup + n_timed)
+        out = {"value": 1e3 / ms, "unit": "frames/s", "ms_per_frame": ms,
+               "config": "512x512 frames, 8x8 grid (win2winaux 120x120 patches, hop 60, frame 256), "
+                         "25x25 drifting motion PSFs, Poisson peak 1000 + N(0, 0.005^2); per frame "
+                         "edgetaper + 10 PG (simplex) + 5 multiplicative steps",
+               "gpu_launches_per_frame": M.launches_per_frame(),
+               "psf_sum_dev": float((M.f.sum(dim=(1, 2)) - 1).abs().max())}
+        if with_unfused:
+            U = UnfusedMFBD(M)
+            ux = torch.empty_like(M.x).copy_(x0)
+            uf = torch.empty_like(M.f).copy_(f0)
+            uy = torch.empty_like(M.y)
+            U.frame(ys[0], ux, uf)
+            torch.cuda.synchronize(dev)
+            ug = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(ug, stream=stream):
+                nx, nf_ = U.frame(uy, ux, uf)
+                ux.copy_(nx)
+                uf.copy_(nf_)
+            torch.cuda.synchronize(dev)
+
+            def unfused(i):
+                uy.copy_(ys[i])
+                ug.replay()
+
+            ums = timed(unfused, args.warmup + max(5, n_timed // 4))
+            out["unfused_gpu"] = {"value": 1e3 / ums, "ms_per_frame": ums, "speedup": ums / ms}
+    return out
+
+
 def barrier(world):
     if world > 1:
         import torch.distributed as dist
@@ -370,7 +446,7 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=list(WORKLOADS), default="cfg2")
+    ap.add_argument("--workload", choices=list(WORKLOADS) + ["mfbd"], default="cfg2")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile", action="store_true",
                     help="short eager run of the step only (for an ncu launch list / capture)")
@@ -380,6 +456,8 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.workload == "mfbd":
+        return main_mfbd(args, world, rank, local)
     w = WORKLOADS[args.workload]
     pixels = w["sx"][0] * w["sx"][1]
     metric = "EFF fwd+adjoint Mpixel/s"
@@ -462,6 +540,11 @@ def main():
         "gpu_launches": 2 * args.steps,
         "clocks": clk,
     }
+    if rank == 0 and world == 1:
+        try:
+            line["mfbd"] = run_mfbd(args, dev, n_timed=20)
+        except Exception as e:  # reported, not fatal to the headline line
+            line["mfbd"] = {"error": repr(e)[:300]}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         r_gpu = R["y"].astype(np.float64) - R["y_obs"]
         t_cpu, reps, cores, (y_o, gx_o, gf_o) = cpu_sample(w, wa, R["x_np"], R["f_np"], R["y_obs"], r_gpu)
@@ -477,6 +560,70 @@ def main():
                                          "note": "adjoints of the same residual y_gpu - y_obs"}
     if rank == 0:
         print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main_mfbd(args, world, rank, local):
+    """``--workload mfbd``: frames/s of the online MFBD loop as the metric."""
+    import torch
+    metric = "MFBD frames/s"
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        from oracle import eff64, mfbd64
+        from vmbd_gb300 import geometry, synth
+        sy, sf, csf = MFBD["sy"], MFBD["sf"], MFBD["csf"]
+        sx = tuple(sy[d] + sf[d] - 1 for d in range(2))
+        wa = geometry.win2winaux(sx, csf, 0.5)
+        g = eff64.Geometry(sx, sf, wa.csf, wa.sw, wa.nhop, "valid")
+        ws = wa.ws.astype(np.float64)
+        xt = synth.blob_edge_image(sx, seed=11)
+        fs = synth.drifting_motion_psfs(4, wa.K, sf, seed=12)
+        cores = os.cpu_count() or 1
+        eff64.set_fft_workers(cores)
+        rng = np.random.default_rng(13)
+        x = np.pad(xt[sf[0] // 2:sf[0] // 2 + sy[0], sf[1] // 2:sf[1] // 2 + sy[1]],
+                   ((sf[0] // 2, sf[0] - 1 - sf[0] // 2), (sf[1] // 2, sf[1] - 1 - sf[1] // 2)), mode="edge")
+        f = np.full((wa.K,) + sf, 1.0 / (sf[0] * sf[1]))
+        state = 1.0
+        times = []
+        for t in range(args.warmup + args.steps):
+            y = eff64.forward(xt, fs[t % 4], g, ws) + 0.005 * rng.standard_normal(g.sy)
+            t0 = time.perf_counter()
+            x, f, state, _ = mfbd64.mfbd_frame(x, f, y, g, ws, MFBD["n_pg"], MFBD["n_mu"], state=state)
+            if t >= args.warmup:
+                times.append(time.perf_counter() - t0)
+        dt = sum(times) / len(times)
+        v = 1.0 / dt
+        print(json.dumps({
+            "impl": "reference", "metric": metric, "value": v, "unit": "frames/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "mfbd"},
+            "cpu_baseline": {"value": v, "unit": "frames/s", "cores": cores, "kind": "port",
+                             "sample": "one frame per step (FP64 NumPy oracle of the frame loop, "
+                                       "scipy.fft over all host cores)"},
+            "e2e": {"value": v, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }))
+        return
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    R = run_mfbd(args, dev, n_timed=args.steps)
+    ms = allreduce_max(R["ms_per_frame"], world, dev)
+    if rank == 0:
+        print(json.dumps({
+            "metric": metric, "value": world * 1e3 / ms, "unit": "frames/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "mfbd", "desc": R["config"], "parallelism": f"replicas x{world}",
+                       "l2": "flushed (256 MB write) before every timed frame"},
+            "unfused_gpu": R.get("unfused_gpu"), "gpu_launches": R["gpu_launches_per_frame"] * args.steps,
+        }))
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()

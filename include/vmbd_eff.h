@@ -150,6 +150,39 @@ int eff_project_psf(float* f, int K, int n, int proj_mode, void* stream);
  * fs [n] and basis [nb, n]. */
 int eff_basis_project(const float* fs, const float* basis, float* w, int nb, int n, void* stream);
 
+/* edgetaper_gpu (gputools.py:643-673, edgetaper.cu:6-31), in place on
+ * [batch, rows, cols]: row i < hy is scaled by wy[i], row i > rows-1-hy by
+ * wy[rows-1-i]; columns likewise with wx.  wy [hy], wx [hx] are DEVICE
+ * tables (the first floor(sf/2) samples of the Bartlett-Hann window over
+ * the product of the two windows' maxima, sf made odd). */
+int eff_edgetaper(float* im, int rows, int cols, const float* wy, int hy, const float* wx, int hx,
+                  int batch, void* stream);
+
+/* eff_adjoint of mask .* y (mask [batch, sy0, sy1]) without forming the
+ * product: Ft(m y) of the multiplicative image step, vmbd_chimney.py:143. */
+int eff_adjoint_masked(const EffPlan* plan, const float* y, const float* mask, const void* fhat,
+                       const void* xhat, float* gx, float* gf, int adj_mode, int batch, void* stream);
+
+/* Online MFBD helpers (vmbd_chimney.py:110-182 with projected-gradient PSF
+ * steps, optGPU.py:134-358):
+ * eff_dots3: out[0] = sum u^2 (na terms), out[2] = sum v^2 (nb terms),
+ *   out[1] = sum u v (min(na, nb) terms), u = a - ap, v = b - bp (ap/bp
+ *   nullable), accumulated in double.
+ * eff_pg_step: per PSF (K of n samples), f_prev <- f, g_prev <- g,
+ *   f <- P_simplex(f - s g), with s from dots: mode 0 exact line search
+ *   (<g,g> / ||Xg||^2 in dots[0], dots[2]), mode 1/2 Barzilai-Borwein
+ *   <dx,dx>/<dx,dg> and <dx,dg>/<dg,dg> (optGPU.py:222-226); state[0] keeps
+ *   the step and is reused when the curvature is not positive.
+ * eff_mu_update: x *= max(num / (den + tol), tol), then x = min(x, max of x
+ *   over the interior [border0, rows-border0) x [border1, cols-border1))
+ *   (vmbd_chimney.py:143-147); xmax_bits is a device scratch word. */
+int eff_dots3(const float* a, const float* ap, long long na, const float* b, const float* bp, long long nb,
+              double* out, void* stream);
+int eff_pg_step(float* f, const float* g, float* f_prev, float* g_prev, int K, int n, const double* dots,
+                int mode, float* state, void* stream);
+int eff_mu_update(float* x, const float* num, const float* den, float tol, int rows, int cols, int border0,
+                  int border1, unsigned* xmax_bits, void* stream);
+
 /* Message for the last non-OK status returned on this thread. */
 const char* eff_last_error(void);
 

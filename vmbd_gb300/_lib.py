@@ -27,7 +27,8 @@ EXPORTS = (
     "eff_psf_spectrum", "eff_image_spectrum", "eff_forward_image", "eff_forward_psf",
     "eff_adjoint", "eff_project_psf", "eff_basis_project", "eff_last_error",
     "eff_forward_both", "eff_adjoint_residual", "eff_loss_grad_workspace_bytes", "eff_loss_grad",
-    "eff_static_scratch_bytes", "eff_loss_grad_static",
+    "eff_static_scratch_bytes", "eff_loss_grad_static", "eff_edgetaper",
+    "eff_adjoint_masked", "eff_dots3", "eff_pg_step", "eff_mu_update",
 )
 
 
@@ -79,6 +80,11 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "eff_loss_grad_workspace_bytes": ([vp, ip], ctypes.c_size_t),
         "eff_loss_grad": ([vp, fp, fp, fp, vp, fp, fp, vp, ctypes.c_size_t, ip, vp], ip),
         "eff_static_scratch_bytes": ([], ctypes.c_size_t),
+        "eff_edgetaper": ([fp, ip, ip, fp, ip, fp, ip, ip, vp], ip),
+        "eff_adjoint_masked": ([vp, fp, fp, vp, vp, fp, fp, ip, ip, vp], ip),
+        "eff_dots3": ([fp, fp, ctypes.c_longlong, fp, fp, ctypes.c_longlong, vp, vp], ip),
+        "eff_pg_step": ([fp, fp, fp, fp, ip, ip, vp, ip, fp, vp], ip),
+        "eff_mu_update": ([fp, fp, fp, ctypes.c_float, ip, ip, ip, ip, vp, vp], ip),
         "eff_loss_grad_static": ([vp, fp, fp, fp, vp, fp, fp, ip, vp], ip),
     }
     for name, (args, res) in sig.items():

@@ -20,6 +20,14 @@ namespace eff {
 cudaError_t launch_project(float* f, int K, int n, int mode, cudaStream_t st);
 cudaError_t launch_basis_project(const float* fs, const float* basis, float* w, int nb, int n,
                                  cudaStream_t st);
+cudaError_t launch_edgetaper(float* im, int rows, int cols, const float* wy, int hy, const float* wx,
+                             int hx, int batch, cudaStream_t st);
+cudaError_t launch_dots3(const float* a, const float* ap, long long na, const float* b, const float* bp,
+                         long long nb, double* out, cudaStream_t st);
+cudaError_t launch_pg_step(float* f, const float* g, float* fp, float* gp, int K, int n, const double* dots,
+                           int mode, float* state, cudaStream_t st);
+cudaError_t launch_mu_update(float* x, const float* num, const float* den, float tol, int rows, int cols,
+                             int b0, int b1, unsigned* xmax_bits, cudaStream_t st);
 }  // namespace eff
 
 struct EffPlan {
@@ -97,7 +105,7 @@ int check_plan(const EffPlan* p, int batch) {
 
 int adjoint_impl(const EffPlan* plan, const float* y, const float* y_obs, const void* fhat,
                  const void* xhat, float* gx, float* gf, double* loss, int adj_mode, int batch,
-                 void* stream) {
+                 void* stream, const float* mask = nullptr) {
   if (int s = check_plan(plan, batch)) return s;
   if (!y || (!gx && !gf)) return fail(EFF_ERR_INVALID, "null argument");
   if (gx && !fhat) return fail(EFF_ERR_INVALID, "image adjoint needs the PSF spectrum");
@@ -109,6 +117,7 @@ int adjoint_impl(const EffPlan* plan, const float* y, const float* y_obs, const 
   eff::Params P = base_params(plan);
   P.y = y;
   P.y_obs = y_obs;
+  P.mask = mask;
   P.b0 = static_cast<const float2*>(fhat);
   P.b1 = static_cast<const float2*>(xhat);
   P.out0 = gx;
@@ -353,6 +362,12 @@ int eff_adjoint_residual(const EffPlan* plan, const float* y, const float* y_obs
   return adjoint_impl(plan, y, y_obs, fhat, xhat, gx, gf, loss, adj_mode, batch, stream);
 }
 
+int eff_adjoint_masked(const EffPlan* plan, const float* y, const float* mask, const void* fhat,
+                       const void* xhat, float* gx, float* gf, int adj_mode, int batch, void* stream) {
+  if (!mask) return fail(EFF_ERR_INVALID, "null mask");
+  return adjoint_impl(plan, y, nullptr, fhat, xhat, gx, gf, nullptr, adj_mode, batch, stream, mask);
+}
+
 int eff_forward_both(const EffPlan* plan, const float* x, const float* f, float* y, void* xhat_out,
                      void* fhat_out, int batch, void* stream) {
   if (int s = check_plan(plan, batch)) return s;
@@ -398,6 +413,44 @@ int eff_basis_project(const float* fs, const float* basis, float* w, int nb, int
   if (!fs || !basis || !w || nb < 1 || n < 1) return fail(EFF_ERR_INVALID, "bad argument");
   cudaError_t e = eff::launch_basis_project(fs, basis, w, nb, n, static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(e, "basis projection launch");
+  return EFF_OK;
+}
+
+int eff_edgetaper(float* im, int rows, int cols, const float* wy, int hy, const float* wx, int hx,
+                  int batch, void* stream) {
+  if (!im || rows < 1 || cols < 1 || batch < 1 || batch > 65535 || hy < 0 || hx < 0 ||
+      (hy > 0 && !wy) || (hx > 0 && !wx) || 2 * hy > rows || 2 * hx > cols)
+    return fail(EFF_ERR_INVALID, "bad argument");
+  cudaError_t e = eff::launch_edgetaper(im, rows, cols, wy, hy, wx, hx, batch, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "edgetaper launch");
+  return EFF_OK;
+}
+
+int eff_dots3(const float* a, const float* ap, long long na, const float* b, const float* bp, long long nb,
+              double* out, void* stream) {
+  if (!a || !b || !out || na < 1 || nb < 1) return fail(EFF_ERR_INVALID, "bad argument");
+  cudaError_t e = eff::launch_dots3(a, ap, na, b, bp, nb, out, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "dots3 launch");
+  return EFF_OK;
+}
+
+int eff_pg_step(float* f, const float* g, float* f_prev, float* g_prev, int K, int n, const double* dots,
+                int mode, float* state, void* stream) {
+  if (!f || !g || !f_prev || !g_prev || !dots || !state || K < 1 || n < 1 || mode < 0 || mode > 2)
+    return fail(EFF_ERR_INVALID, "bad argument");
+  if (n > 12288) return fail(EFF_ERR_UNSUPPORTED, "PSF larger than 12288 samples");
+  cudaError_t e = eff::launch_pg_step(f, g, f_prev, g_prev, K, n, dots, mode, state, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "pg_step launch");
+  return EFF_OK;
+}
+
+int eff_mu_update(float* x, const float* num, const float* den, float tol, int rows, int cols, int border0,
+                  int border1, unsigned* xmax_bits, void* stream) {
+  if (!x || !num || !den || !xmax_bits || rows < 1 || cols < 1 || border0 < 0 || border1 < 0)
+    return fail(EFF_ERR_INVALID, "bad argument");
+  cudaError_t e = eff::launch_mu_update(x, num, den, tol, rows, cols, border0, border1, xmax_bits,
+                                        static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "mu_update launch");
   return EFF_OK;
 }
 

@@ -45,6 +45,7 @@ struct Params {
   const float* f;          // PSFs [K, sf0, sf1]
   const float* y;          // output-side image [sy0, sy1] (adjoint input)
   const float* y_obs;      // adjoint: when set, the input is y - y_obs
+  const float* mask;       // adjoint: when set, the input is multiplied by mask [sy0, sy1]
   const float2* b0;        // cached spectrum: F-hat (fwd image / adj image) or X-hat (fwd psf)
   const float2* b1;        // cached spectrum: X-hat (adj psf)
   float2* a_out;           // spectrum of operand A (optional)
@@ -105,6 +106,7 @@ struct Patch {
   const float* f;
   const float* y;
   const float* y_obs;
+  const float* mask;
 };
 
 // Operand value at frame position (r, c).
@@ -126,6 +128,7 @@ __device__ __forceinline__ float operand(const Params& P, const Patch& T, int r,
     const long long o = (long long)i * P.sy1 + j;
     float v = __ldg(T.y + o);
     if (T.y_obs) v -= __ldg(T.y_obs + o);
+    if (T.mask) v *= __ldg(T.mask + o);
     return v;
   }
 }
@@ -367,6 +370,7 @@ __global__ void __launch_bounds__(max_threads(N)) eff_kernel(Params P) {
   T.f = P.f ? P.f + b * P.f_bs : nullptr;
   T.y = P.y ? P.y + b * P.y_bs : nullptr;
   T.y_obs = P.y_obs ? P.y_obs + b * P.y_bs : nullptr;
+  T.mask = P.mask ? P.mask + b * P.y_bs : nullptr;
   const long long spec_patch = (long long)(N / 2 + 1) * N;
   const long long spec_off = b * P.spec_bs + T.k * spec_patch;
   const float2* b0 = P.b0 ? P.b0 + spec_off : nullptr;

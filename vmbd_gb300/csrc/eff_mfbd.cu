@@ -1,0 +1,183 @@
+// Small fused kernels of the online multi-frame blind deconvolution step.
+//
+// PSF step: projected gradient with Barzilai-Borwein step sizes (the step
+// rule of PBB, optGPU.py:222-226, alternating <dx,dx>/<dx,dg> and
+// <dx,dg>/<dg,dg>) and the Euclidean simplex projection; the first step of
+// a frame uses the exact line search <g,g>/||Xg||^2 of the quadratic.
+// Image step: the multiplicative update of vmbd_chimney.py:143-147,
+// x *= max(Ft(m y) / (Ft(m F x) + tol), tol), then x <= max over the
+// interior of x.
+#include <cuda_runtime.h>
+
+namespace eff {
+
+constexpr int kMfbdThreads = 256;
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// out[0] += sum (a-ap)^2 over na, out[2] += sum (b-bp)^2 over nb,
+// out[1] += sum (a-ap)(b-bp) over min(na, nb); ap / bp may be null.
+__global__ void __launch_bounds__(kMfbdThreads) dots3_kernel(const float* a, const float* ap, long long na,
+                                                             const float* b, const float* bp, long long nb,
+                                                             double* out) {
+  double s0 = 0, s1 = 0, s2 = 0;
+  const long long n = na > nb ? na : nb;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const float u = i < na ? a[i] - (ap ? ap[i] : 0.f) : 0.f;
+    const float v = i < nb ? b[i] - (bp ? bp[i] : 0.f) : 0.f;
+    s0 += double(u) * u;
+    s1 += double(u) * v;
+    s2 += double(v) * v;
+  }
+  s0 = warp_sum(s0);
+  s1 = warp_sum(s1);
+  s2 = warp_sum(s2);
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(out, s0);
+    atomicAdd(out + 1, s1);
+    atomicAdd(out + 2, s2);
+  }
+}
+
+// Deterministic block sum (float2), every thread gets the totals.
+__device__ __forceinline__ float2 block_sum2f(float a, float b, float2* red) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, o);
+    b += __shfl_xor_sync(0xffffffffu, b, o);
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) red[w] = make_float2(a, b);
+  __syncthreads();
+  const int nw = blockDim.x >> 5;
+  float2 t = l < nw ? red[l] : make_float2(0.f, 0.f);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    t.x += __shfl_xor_sync(0xffffffffu, t.x, o);
+    t.y += __shfl_xor_sync(0xffffffffu, t.y, o);
+  }
+  return t;
+}
+
+// Step size from the dot products.  mode 0: exact line search
+// dots = (<g,g>, ., ||Xg||^2); mode 1/2: BB1/BB2 with dots = (<dx,dx>,
+// <dx,dg>, <dg,dg>); a non-positive curvature keeps the previous step.
+__device__ __forceinline__ float pg_step_size(const double* dots, int mode, float prev) {
+  double s;
+  if (mode == 0) s = dots[2] > 0 ? dots[0] / dots[2] : 0.0;
+  else if (dots[1] <= 0) s = prev;
+  else if (mode == 1) s = dots[0] / dots[1];
+  else s = dots[2] > 0 ? dots[1] / dots[2] : prev;
+  if (!(s > 0) || !isfinite(s)) s = prev;
+  return (float)s;
+}
+
+// One PSF per CTA: fp <- f, gp <- g, f <- P_simplex(f - s g).  state[0] holds
+// the step size (written by CTA 0).
+__global__ void __launch_bounds__(kMfbdThreads) pg_step_kernel(float* f, const float* g, float* fp, float* gp,
+                                                               int n, const double* dots, int mode,
+                                                               float* state) {
+  extern __shared__ float v[];
+  __shared__ float2 red[32];
+  const float s = pg_step_size(dots, mode, state[0]);
+  const long long base = (long long)blockIdx.x * n;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const float fi = f[base + i], gi = g[base + i];
+    fp[base + i] = fi;
+    gp[base + i] = gi;
+    v[i] = fi - s * gi;
+  }
+  __syncthreads();
+  if (blockIdx.x == 0 && threadIdx.x == 0) state[0] = s;
+  // Michelot's active-set iteration for the simplex projection.
+  float sum = 0.f;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) sum += v[i];
+  float2 t = block_sum2f(sum, 0.f, red);
+  float tau = (t.x - 1.f) / float(n);
+  int count = n;
+  for (int it = 0; it <= n; ++it) {
+    float ss = 0.f, cc = 0.f;
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+      if (v[i] > tau) {
+        ss += v[i];
+        cc += 1.f;
+      }
+    t = block_sum2f(ss, cc, red);
+    const int c = int(t.y + 0.5f);
+    if (c == 0) break;
+    const float tn = (t.x - 1.f) / t.y;
+    if (c == count) {
+      tau = tn;
+      break;
+    }
+    count = c;
+    tau = tn;
+  }
+  for (int i = threadIdx.x; i < n; i += blockDim.x) f[base + i] = fmaxf(v[i] - tau, 0.f);
+}
+
+// x *= max(num / (den + tol), tol); xmax_bits <- max over the interior
+// [b0, rows-b0) x [b1, cols-b1) of the updated x (x >= 0, so the float bit
+// patterns order like the values).
+__global__ void __launch_bounds__(kMfbdThreads) mu_update_kernel(float* x, const float* num, const float* den,
+                                                                 float tol, int rows, int cols, int b0, int b1,
+                                                                 unsigned* xmax_bits) {
+  const long long n = (long long)rows * cols;
+  float m = 0.f;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x) {
+    const float fac = fmaxf(num[t] / (den[t] + tol), tol);
+    const float xv = x[t] * fac;
+    x[t] = xv;
+    const int i = int(t / cols), j = int(t % cols);
+    if (i >= b0 && i < rows - b0 && j >= b1 && j < cols - b1) m = fmaxf(m, xv);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(xmax_bits, __float_as_uint(fmaxf(m, 0.f)));
+}
+
+__global__ void __launch_bounds__(kMfbdThreads) clamp_max_kernel(float* x, long long n, const unsigned* xmax_bits) {
+  const float mx = __uint_as_float(*xmax_bits);
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x)
+    x[t] = fminf(x[t], mx);
+}
+
+static int grid_for(long long n) {
+  const long long b = (n + kMfbdThreads - 1) / kMfbdThreads;
+  return (int)(b < 1216 ? (b < 1 ? 1 : b) : 1216);
+}
+
+cudaError_t launch_dots3(const float* a, const float* ap, long long na, const float* b, const float* bp,
+                         long long nb, double* out, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(out, 0, 3 * sizeof(double), st);
+  if (e != cudaSuccess) return e;
+  dots3_kernel<<<grid_for(na > nb ? na : nb), kMfbdThreads, 0, st>>>(a, ap, na, b, bp, nb, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pg_step(float* f, const float* g, float* fp, float* gp, int K, int n, const double* dots,
+                           int mode, float* state, cudaStream_t st) {
+  pg_step_kernel<<<K, kMfbdThreads, n * sizeof(float), st>>>(f, g, fp, gp, n, dots, mode, state);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mu_update(float* x, const float* num, const float* den, float tol, int rows, int cols,
+                             int b0, int b1, unsigned* xmax_bits, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(xmax_bits, 0, sizeof(unsigned), st);
+  if (e != cudaSuccess) return e;
+  const long long n = (long long)rows * cols;
+  mu_update_kernel<<<grid_for(n), kMfbdThreads, 0, st>>>(x, num, den, tol, rows, cols, b0, b1, xmax_bits);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  clamp_max_kernel<<<grid_for(n), kMfbdThreads, 0, st>>>(x, n, xmax_bits);
+  return cudaGetLastError();
+}
+
+}  // namespace eff

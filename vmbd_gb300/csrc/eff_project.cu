@@ -109,3 +109,35 @@ cudaError_t launch_basis_project(const float* fs, const float* basis, float* w, 
 }
 
 }  // namespace eff
+
+namespace eff {
+
+// Edge taper in place (edgetaper.cu:6-31 via edgetaper_gpu,
+// gputools.py:643-673): rows i < hy are scaled by wy[i], rows
+// i > rows-1-hy by wy[rows-1-i], likewise columns with wx; the interior is
+// untouched.  Both images of a batch share the tables.
+__global__ void edgetaper_kernel(float* im, int rows, int cols, const float* __restrict__ wy, int hy,
+                                 const float* __restrict__ wx, int hx) {
+  const long long plane = (long long)rows * cols;
+  float* p = im + blockIdx.y * plane;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < plane;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int i = int(t / cols), j = int(t - (long long)(t / cols) * cols);
+    float s = 1.f;
+    if (i < hy) s = __ldg(wy + i);
+    else if (i > rows - 1 - hy) s = __ldg(wy + rows - 1 - i);
+    if (j < hx) s *= __ldg(wx + j);
+    else if (j > cols - 1 - hx) s *= __ldg(wx + cols - 1 - j);
+    if (s != 1.f) p[t] *= s;
+  }
+}
+
+cudaError_t launch_edgetaper(float* im, int rows, int cols, const float* wy, int hy, const float* wx,
+                             int hx, int batch, cudaStream_t st) {
+  const long long plane = (long long)rows * cols;
+  const int blocks = (int)((plane + 255) / 256 < 1184 ? (plane + 255) / 256 : 1184);
+  edgetaper_kernel<<<dim3(blocks, batch), 256, 0, st>>>(im, rows, cols, wy, hy, wx, hx);
+  return cudaGetLastError();
+}
+
+}  // namespace eff

@@ -107,3 +107,100 @@ class UnfusedEff:
         gx = self._ola(zx.contiguous(), self.sw, self.sx)
         zf = torch.fft.ifft2(yh * xhat.conj()).real[:, :self.sf[0], :self.sf[1]].contiguous()
         return gx, zf
+
+    # -- pieces used by the unfused MFBD comparator ---------------------------
+    def forward_from_spectra(self, xh, fh):
+        ys = torch.fft.ifft2(fh * xh)
+        yre = ys.real[:, :self.E[0], :self.E[1]].contiguous()
+        yfull = self._ola(yre, self.E, self.full)
+        o = self.off
+        out = torch.zeros(self.sy, device=xh.device, dtype=torch.float32)
+        h = min(self.sy[0], self.full[0] - o[0])
+        w = min(self.sy[1], self.full[1] - o[1])
+        out[:h, :w] = yfull[o[0]:o[0] + h, o[1]:o[1] + w]
+        return out
+
+    def frames_spectrum(self, y):
+        N = self.N
+        o = self.off
+        emb = torch.zeros(self.full, device=y.device, dtype=torch.float32)
+        h = min(self.sy[0], self.full[0] - o[0])
+        w = min(self.sy[1], self.full[1] - o[1])
+        emb[o[0]:o[0] + h, o[1]:o[1] + w] = y[:h, :w]
+        fr = self._chop(emb, self.ie, self.je, self.E)
+        fr = F.pad(fr, (0, N - self.E[1], 0, N - self.E[0]))
+        return torch.fft.fft2(fr.to(torch.complex64))
+
+    def adjoint_image_only(self, yh, fhat):
+        zx = torch.fft.ifft2(yh * fhat.conj()).real[:, :self.sw[0], :self.sw[1]] * self.ws
+        return self._ola(zx.contiguous(), self.sw, self.sx)
+
+    def adjoint_psf_only(self, yh, xhat):
+        return torch.fft.ifft2(yh * xhat.conj()).real[:, :self.sf[0], :self.sf[1]].contiguous()
+
+
+def simplex_project_torch(v):
+    """Euclidean projection of each row of v [K, n] onto the unit simplex
+    (Duchi et al. 2008, sort-based)."""
+    K, n = v.shape
+    u, _ = torch.sort(v, dim=1, descending=True)
+    css = torch.cumsum(u, 1) - 1
+    j = torch.arange(1, n + 1, device=v.device, dtype=v.dtype)
+    cond = (u - css / j) > 0
+    rho = (cond.to(v.dtype) * j).amax(1)
+    tau = css.gather(1, (rho.long() - 1).clamp_min(0)[:, None])[:, 0] / rho
+    return (v - tau[:, None]).clamp_min(0)
+
+
+class UnfusedMFBD:
+    """The same frame loop as ``vmbd_gb300.mfbd.OnlineMFBD`` built from the
+    unfused per-stage operator and plain torch ops (comparator only)."""
+
+    def __init__(self, mfbd):
+        self.m = mfbd
+        self.U = UnfusedEff(mfbd.winaux, mfbd.sf, N=mfbd.plan.N, device=mfbd.device)
+        from .gputools import edgetaper_tables
+        wy, wx = edgetaper_tables(mfbd.sf)
+        R, C = mfbd.sy
+        ry = torch.ones(R, device=mfbd.device)
+        cx = torch.ones(C, device=mfbd.device)
+        hy, hx = len(wy), len(wx)
+        ry[:hy] = torch.from_numpy(wy).to(mfbd.device)
+        ry[R - hy:] = torch.from_numpy(wy[::-1].copy()).to(mfbd.device)
+        cx[:hx] = torch.from_numpy(wx).to(mfbd.device)
+        cx[C - hx:] = torch.from_numpy(wx[::-1].copy()).to(mfbd.device)
+        self.taper = ry[:, None] * cx[None, :]
+        self.state = torch.ones((), device=mfbd.device)
+
+    def frame(self, y, x, f):
+        m, U = self.m, self.U
+        K, n = m.winaux.K, m.n
+        y = y * self.taper
+        mask = (y < 1).float()
+        xh = U.image_spectrum(x)
+        yh_obs = None
+        fp = gp = None
+        for k in range(m.n_pg):
+            fh = U.psf_spectrum(f)
+            yp = U.forward_from_spectra(xh, fh)
+            g = U.adjoint_psf_only(U.frames_spectrum(yp - y), xh)
+            if k == 0:
+                xg = U.forward_from_spectra(xh, U.psf_spectrum(g))
+                s = (g * g).sum() / (xg * xg).sum()
+            else:
+                dx, dg = (f - fp).flatten(), (g - gp).flatten()
+                a, b, c = (dx * dx).sum(), (dx * dg).sum(), (dg * dg).sum()
+                cand = a / b if k % 2 == 1 else b / c
+                s = torch.where((b > 0) & torch.isfinite(cand) & (cand > 0), cand, self.state)
+            self.state = s
+            fp, gp = f, g
+            f = simplex_project_torch((f - s * g).reshape(K, n)).reshape(f.shape)
+        fh = U.psf_spectrum(f)
+        num = U.adjoint_image_only(U.frames_spectrum(mask * y), fh)
+        s0, s1 = m.sf
+        for _ in range(m.n_mu):
+            yp = U.forward_from_spectra(U.image_spectrum(x), fh)
+            den = U.adjoint_image_only(U.frames_spectrum(mask * yp), fh)
+            x = x * torch.clamp_min(num / (den + m.tol), m.tol)
+            x = torch.minimum(x, x[s0:x.shape[0] - s0, s1:x.shape[1] - s1].max())
+        return x, f
