@@ -173,15 +173,23 @@ int eff_adjoint_masked(const EffPlan* plan, const float* y, const float* mask, c
  *   (<g,g> / ||Xg||^2 in dots[0], dots[2]), mode 1/2 Barzilai-Borwein
  *   <dx,dx>/<dx,dg> and <dx,dg>/<dg,dg> (optGPU.py:222-226); state[0] keeps
  *   the step and is reused when the curvature is not positive.
- * eff_mu_update: x *= max(num / (den + tol), tol), then x = min(x, max of x
- *   over the interior [border0, rows-border0) x [border1, cols-border1))
- *   (vmbd_chimney.py:143-147); xmax_bits is a device scratch word. */
+ * eff_max_nonneg: *out_bits = max(0, max a) as float bits (device word).
+ * eff_mu_update: x *= max(num' / (den + tol), tol) with num' = num where
+ *   num > floor_rel * max(num) (num_max_bits from eff_max_nonneg) and 0
+ *   elsewhere, then x = min(x, max of x over the interior [border0,
+ *   rows-border0) x [border1, cols-border1)) (vmbd_chimney.py:143-147).
+ *   Where no data reaches a pixel num and den are 0 in exact arithmetic (the
+ *   factor is tol) but FP32 transform noise well above tol = 1e-10; the
+ *   floor (1e-6 in vmbd_gb300.mfbd) restores the exact-arithmetic factor.
+ *   xmax_bits is a device scratch word. */
 int eff_dots3(const float* a, const float* ap, long long na, const float* b, const float* bp, long long nb,
               double* out, void* stream);
 int eff_pg_step(float* f, const float* g, float* f_prev, float* g_prev, int K, int n, const double* dots,
                 int mode, float* state, void* stream);
+int eff_max_nonneg(const float* a, long long n, unsigned* out_bits, void* stream);
 int eff_mu_update(float* x, const float* num, const float* den, float tol, int rows, int cols, int border0,
-                  int border1, unsigned* xmax_bits, void* stream);
+                  int border1, const unsigned* num_max_bits, float floor_rel, unsigned* xmax_bits,
+                  void* stream);
 
 /* Message for the last non-OK status returned on this thread. */
 const char* eff_last_error(void);

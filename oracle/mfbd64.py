@@ -7,7 +7,9 @@ projected gradient: PBB's Barzilai-Borwein step rule (optGPU.py:222-226,
 BB1 on odd, BB2 on even iterations after an exact line search on the first)
 and the Euclidean simplex projection (``eff64.simplex_project``) in place of
 L-BFGS-B's bounds + ``normalize``; then ``n_mu`` multiplicative image steps
-(vmbd_chimney.py:143-147).  Adjoints are the exact transposes.
+(vmbd_chimney.py:143-147), with F^T(m y) below ``num_floor`` of its maximum
+taken as 0 (where no data reaches a pixel it is 0 in exact arithmetic; the
+FP32 kernels see transform noise there).  Adjoints are the exact transposes.
 """
 from __future__ import annotations
 
@@ -34,8 +36,10 @@ def step_size(dots, mode, prev):
     return s
 
 
-def mfbd_frame(x, f, y, g: eff64.Geometry, ws, n_pg=10, n_mu=5, tol=1e-10, taper=True, state=1.0):
-    """One frame: returns (x, f, state, psf_objective_per_iteration)."""
+def mfbd_frame(x, f, y, g: eff64.Geometry, ws, n_pg=10, n_mu=5, tol=1e-10, taper=True, state=1.0,
+               num_floor=1e-6, out=None):
+    """One frame: returns (x, f, state, psf_objective_per_iteration); when
+    ``out`` is a dict it also receives the image-step numerator ``num``."""
     y = np.asarray(y, np.float64)
     if taper:
         y = eff64.edgetaper(y, g.sf)
@@ -62,6 +66,10 @@ def mfbd_frame(x, f, y, g: eff64.Geometry, ws, n_pg=10, n_mu=5, tol=1e-10, taper
         f = eff64.simplex_project(f - s * gr)
     objs.append(0.5 * np.sum((eff64.forward(x, f, g, ws) - y) ** 2))
     num = eff64.adjoint_image(mask * y, f, g, ws)
+    # values below num_floor * max are transform noise (0 in exact arithmetic)
+    num = np.where(num > num_floor * max(num.max(), 0.0), num, 0.0)
+    if out is not None:
+        out["num"] = num
     s0, s1 = g.sf
     for _ in range(n_mu):
         yp = eff64.forward(x, f, g, ws)

@@ -28,7 +28,7 @@ EXPORTS = (
     "eff_adjoint", "eff_project_psf", "eff_basis_project", "eff_last_error",
     "eff_forward_both", "eff_adjoint_residual", "eff_loss_grad_workspace_bytes", "eff_loss_grad",
     "eff_static_scratch_bytes", "eff_loss_grad_static", "eff_edgetaper",
-    "eff_adjoint_masked", "eff_dots3", "eff_pg_step", "eff_mu_update",
+    "eff_adjoint_masked", "eff_dots3", "eff_pg_step", "eff_mu_update", "eff_max_nonneg",
 )
 
 
@@ -84,7 +84,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "eff_adjoint_masked": ([vp, fp, fp, vp, vp, fp, fp, ip, ip, vp], ip),
         "eff_dots3": ([fp, fp, ctypes.c_longlong, fp, fp, ctypes.c_longlong, vp, vp], ip),
         "eff_pg_step": ([fp, fp, fp, fp, ip, ip, vp, ip, fp, vp], ip),
-        "eff_mu_update": ([fp, fp, fp, ctypes.c_float, ip, ip, ip, ip, vp, vp], ip),
+        "eff_max_nonneg": ([fp, ctypes.c_longlong, vp, vp], ip),
+        "eff_mu_update": ([fp, fp, fp, ctypes.c_float, ip, ip, ip, ip, vp, ctypes.c_float, vp, vp], ip),
         "eff_loss_grad_static": ([vp, fp, fp, fp, vp, fp, fp, ip, vp], ip),
     }
     for name, (args, res) in sig.items():

@@ -26,8 +26,10 @@ cudaError_t launch_dots3(const float* a, const float* ap, long long na, const fl
                          long long nb, double* out, cudaStream_t st);
 cudaError_t launch_pg_step(float* f, const float* g, float* fp, float* gp, int K, int n, const double* dots,
                            int mode, float* state, cudaStream_t st);
+cudaError_t launch_max_nonneg(const float* a, long long n, unsigned* out_bits, cudaStream_t st);
 cudaError_t launch_mu_update(float* x, const float* num, const float* den, float tol, int rows, int cols,
-                             int b0, int b1, unsigned* xmax_bits, cudaStream_t st);
+                             int b0, int b1, const unsigned* num_max_bits, float floor_rel, unsigned* xmax_bits,
+                             cudaStream_t st);
 }  // namespace eff
 
 struct EffPlan {
@@ -444,12 +446,21 @@ int eff_pg_step(float* f, const float* g, float* f_prev, float* g_prev, int K, i
   return EFF_OK;
 }
 
+int eff_max_nonneg(const float* a, long long n, unsigned* out_bits, void* stream) {
+  if (!a || !out_bits || n < 1) return fail(EFF_ERR_INVALID, "bad argument");
+  cudaError_t e = eff::launch_max_nonneg(a, n, out_bits, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "max launch");
+  return EFF_OK;
+}
+
 int eff_mu_update(float* x, const float* num, const float* den, float tol, int rows, int cols, int border0,
-                  int border1, unsigned* xmax_bits, void* stream) {
-  if (!x || !num || !den || !xmax_bits || rows < 1 || cols < 1 || border0 < 0 || border1 < 0)
+                  int border1, const unsigned* num_max_bits, float floor_rel, unsigned* xmax_bits,
+                  void* stream) {
+  if (!x || !num || !den || !xmax_bits || !num_max_bits || rows < 1 || cols < 1 || border0 < 0 ||
+      border1 < 0 || !(floor_rel >= 0.f))
     return fail(EFF_ERR_INVALID, "bad argument");
-  cudaError_t e = eff::launch_mu_update(x, num, den, tol, rows, cols, border0, border1, xmax_bits,
-                                        static_cast<cudaStream_t>(stream));
+  cudaError_t e = eff::launch_mu_update(x, num, den, tol, rows, cols, border0, border1, num_max_bits,
+                                        floor_rel, xmax_bits, static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(e, "mu_update launch");
   return EFF_OK;
 }

@@ -122,17 +122,35 @@ __global__ void __launch_bounds__(kMfbdThreads) pg_step_kernel(float* f, const f
   for (int i = threadIdx.x; i < n; i += blockDim.x) f[base + i] = fmaxf(v[i] - tau, 0.f);
 }
 
+// out_bits <- max(0, max_i a[i]) as float bits (non-negative floats order
+// like their bit patterns).
+__global__ void __launch_bounds__(kMfbdThreads) max_nonneg_kernel(const float* a, long long n, unsigned* out_bits) {
+  float m = 0.f;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x)
+    m = fmaxf(m, a[t]);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out_bits, __float_as_uint(m));
+}
+
 // x *= max(num / (den + tol), tol); xmax_bits <- max over the interior
 // [b0, rows-b0) x [b1, cols-b1) of the updated x (x >= 0, so the float bit
-// patterns order like the values).
+// patterns order like the values).  num below floor * max(num) is taken as
+// 0: where no data reaches a pixel, num and den are 0 in exact arithmetic
+// (factor tol) but FP32 transform noise of ~1e-8 of the image scale, far
+// above tol, and their ratio would be noise over noise.
 __global__ void __launch_bounds__(kMfbdThreads) mu_update_kernel(float* x, const float* num, const float* den,
                                                                  float tol, int rows, int cols, int b0, int b1,
+                                                                 const unsigned* num_max_bits, float floor_rel,
                                                                  unsigned* xmax_bits) {
   const long long n = (long long)rows * cols;
+  const float nfloor = floor_rel * __uint_as_float(*num_max_bits);
   float m = 0.f;
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
        t += (long long)gridDim.x * blockDim.x) {
-    const float fac = fmaxf(num[t] / (den[t] + tol), tol);
+    const float nu = num[t] > nfloor ? num[t] : 0.f;
+    const float fac = fmaxf(nu / (den[t] + tol), tol);
     const float xv = x[t] * fac;
     x[t] = xv;
     const int i = int(t / cols), j = int(t % cols);
@@ -169,12 +187,21 @@ cudaError_t launch_pg_step(float* f, const float* g, float* fp, float* gp, int K
   return cudaGetLastError();
 }
 
+cudaError_t launch_max_nonneg(const float* a, long long n, unsigned* out_bits, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(out_bits, 0, sizeof(unsigned), st);
+  if (e != cudaSuccess) return e;
+  max_nonneg_kernel<<<grid_for(n), kMfbdThreads, 0, st>>>(a, n, out_bits);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_mu_update(float* x, const float* num, const float* den, float tol, int rows, int cols,
-                             int b0, int b1, unsigned* xmax_bits, cudaStream_t st) {
+                             int b0, int b1, const unsigned* num_max_bits, float floor_rel, unsigned* xmax_bits,
+                             cudaStream_t st) {
   cudaError_t e = cudaMemsetAsync(xmax_bits, 0, sizeof(unsigned), st);
   if (e != cudaSuccess) return e;
   const long long n = (long long)rows * cols;
-  mu_update_kernel<<<grid_for(n), kMfbdThreads, 0, st>>>(x, num, den, tol, rows, cols, b0, b1, xmax_bits);
+  mu_update_kernel<<<grid_for(n), kMfbdThreads, 0, st>>>(x, num, den, tol, rows, cols, b0, b1, num_max_bits,
+                                                          floor_rel, xmax_bits);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   clamp_max_kernel<<<grid_for(n), kMfbdThreads, 0, st>>>(x, n, xmax_bits);
   return cudaGetLastError();

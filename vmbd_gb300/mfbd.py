@@ -15,7 +15,9 @@ graph):
    Barzilai-Borwein steps after it (PBB's rule, optGPU.py:222-226), Euclidean
    projection of every PSF onto the unit simplex;
 3. ``n_mu`` multiplicative image steps x *= max(F^T(m y) / (F^T(m F x) + tol),
-   tol), x <= max of x over the interior (vmbd_chimney.py:143-147).
+   tol), x <= max of x over the interior (vmbd_chimney.py:143-147), with
+   F^T(m y) below 1e-6 of its maximum taken as 0 (FP32 transform noise where
+   no data reaches a pixel; exact arithmetic gives 0 there).
 """
 from __future__ import annotations
 
@@ -31,6 +33,10 @@ from .gputools import EdgeTaper, impad_gpu
 
 
 class OnlineMFBD:
+    # Fraction of max F^T(m y) below which it is FP32 transform noise (see
+    # eff_mu_update in include/vmbd_eff.h).
+    NUM_FLOOR = 1e-6
+
     def __init__(self, sy, sf, csf, overlap=0.5, n_pg=10, n_mu=5, tol=1e-10, taper=True,
                  device=None, sw=None, nhop=None, adjoint="exact"):
         self.sy = (int(sy[0]), int(sy[1]))
@@ -68,6 +74,7 @@ class OnlineMFBD:
         self.loss = z(1, torch.float64)
         self.state = torch.ones(1, dtype=torch.float32, device=dev)
         self.xmax = z(1, torch.int32)
+        self.nummax = z(1, torch.int32)
         self.taper = EdgeTaper(self.sf, dev) if taper else None
 
     # ------------------------------------------------------------------
@@ -112,17 +119,19 @@ class OnlineMFBD:
         mode = _lib.ADJ_EXACT if self.adjoint == "exact" else _lib.ADJ_REFERENCE
         self._check(L.eff_adjoint_masked(P._h, _ptr(self.y), _ptr(self.mask), _ptr(self.fhat), None,
                                          _ptr(self.num), None, mode, 1, st))
+        self._check(L.eff_max_nonneg(_ptr(self.num), self.sx[0] * self.sx[1], _ptr(self.nummax), st))
         for _ in range(self.n_mu):
             P.forward_image(self.x, self.fhat, out=self.ypred)
             self._check(L.eff_adjoint_masked(P._h, _ptr(self.ypred), _ptr(self.mask), _ptr(self.fhat),
                                              None, _ptr(self.den), None, mode, 1, st))
             self._check(L.eff_mu_update(_ptr(self.x), _ptr(self.num), _ptr(self.den),
                                         ctypes.c_float(self.tol), self.sx[0], self.sx[1], self.sf[0],
-                                        self.sf[1], _ptr(self.xmax), st))
+                                        self.sf[1], _ptr(self.nummax), ctypes.c_float(self.NUM_FLOOR),
+                                        _ptr(self.xmax), st))
 
     def launches_per_frame(self) -> int:
         """Kernels of this library one frame launches."""
-        return ((1 if self.taper else 0) + 1 + self.n_pg * 4 + 1 + 1 + 1 + self.n_mu * 4)
+        return ((1 if self.taper else 0) + 1 + self.n_pg * 4 + 1 + 1 + 1 + 1 + self.n_mu * 4)
 
 
 def make_sequence(plan: EffPlan, n_frames: int, seed: int = 3, peak: float = 1000.0, sigma: float = 0.005):
