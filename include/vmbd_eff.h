@@ -191,6 +191,12 @@ int eff_mu_update(float* x, const float* num, const float* den, float tol, int r
                   int border1, const unsigned* num_max_bits, float floor_rel, unsigned* xmax_bits,
                   void* stream);
 
+/* How many CTAs process one patch, for all plans of the process:
+ * 0 (default) per call -- a 2-CTA thread-block cluster when one CTA's frame
+ * does not fit in shared memory or when twice the grid still fits on the
+ * GPU's SMs at once; 1 always one CTA (where it fits); 2 always a cluster. */
+int eff_set_cluster_mode(int mode);
+
 /* Message for the last non-OK status returned on this thread. */
 const char* eff_last_error(void);
 

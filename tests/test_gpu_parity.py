@@ -87,8 +87,18 @@ CASES = {
 }
 
 
+@pytest.fixture(params=[1, 2], ids=["cta", "cluster2"])
+def cluster_mode(request, cuda):
+    """Run a test with one CTA per patch, then with a 2-CTA cluster."""
+    from vmbd_gb300 import _lib
+    lib = _lib.load()
+    _lib.check(lib.eff_set_cluster_mode(request.param))
+    yield request.param
+    _lib.check(lib.eff_set_cluster_mode(0))
+
+
 @pytest.mark.parametrize("name", list(CASES))
-def test_operator_matches_fp64_oracle(cuda, name):
+def test_operator_matches_fp64_oracle(cuda, cluster_mode, name):
     from vmbd_gb300.eff import EffPlan
     wa, g, x, f, r = make(**CASES[name])
     plan = EffPlan(wa, g.sf, g.mode, device=cuda)
@@ -124,6 +134,25 @@ def test_operator_matches_fp64_oracle(cuda, name):
         gx, gf = plan.adjoint(t(r, cuda), fh, xh, adjoint="reference")
         assert rel(gx.cpu().numpy(), eff64.adjoint_image(r, f, g, ws, exact=False)) < TOL
         assert rel(gf.cpu().numpy(), eff64.adjoint_psf(r, x, g, ws, exact=False)) < TOL
+
+
+def test_2048_stress_workload(cuda):
+    """2048x2048 image, 16x16 grid of 192x192 patches (hop 96), 41x41 motion
+    PSFs, frame 256: one CTA's frame would need 240 KB of shared memory, so
+    every call runs on 2-CTA clusters.  Forward against the FP64 oracle at
+    full size; both adjoints through the adjoint identity."""
+    from vmbd_gb300.eff import EffPlan
+    wa, g, x, f, r = make(sx=(2048, 2048), csf=(16, 16), sf=(41, 41), sw=(192, 192), hop=(96, 96),
+                          kind="motion", seed=21)
+    plan = EffPlan(wa, g.sf, device=cuda)
+    assert plan.N == 256
+    xh, fh = plan.empty_spectrum(), plan.empty_spectrum()
+    y = plan.forward_both(t(x, cuda), t(f, cuda), xhat_out=xh, fhat_out=fh)
+    assert rel(y.cpu().numpy(), eff64.forward(x, f, g, wa.ws.astype(np.float64))) < TOL
+    gx, gf = plan.adjoint(t(r, cuda), fh, xh)
+    lhs = np.vdot(y.double().cpu().numpy(), r)
+    assert abs(lhs - np.vdot(x, gx.double().cpu().numpy())) < 1e-5 * abs(lhs)
+    assert abs(lhs - np.vdot(f, gf.double().cpu().numpy())) < 1e-5 * abs(lhs)
 
 
 def test_psf_spectrum_matches_numpy_fft(cuda):

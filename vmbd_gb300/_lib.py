@@ -29,6 +29,7 @@ EXPORTS = (
     "eff_forward_both", "eff_adjoint_residual", "eff_loss_grad_workspace_bytes", "eff_loss_grad",
     "eff_static_scratch_bytes", "eff_loss_grad_static", "eff_edgetaper",
     "eff_adjoint_masked", "eff_dots3", "eff_pg_step", "eff_mu_update", "eff_max_nonneg",
+    "eff_set_cluster_mode",
 )
 
 
@@ -85,6 +86,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "eff_dots3": ([fp, fp, ctypes.c_longlong, fp, fp, ctypes.c_longlong, vp, vp], ip),
         "eff_pg_step": ([fp, fp, fp, fp, ip, ip, vp, ip, fp, vp], ip),
         "eff_max_nonneg": ([fp, ctypes.c_longlong, vp, vp], ip),
+        "eff_set_cluster_mode": ([ip], ip),
         "eff_mu_update": ([fp, fp, fp, ctypes.c_float, ip, ip, ip, ip, vp, ctypes.c_float, vp, vp], ip),
         "eff_loss_grad_static": ([vp, fp, fp, fp, vp, fp, fp, ip, vp], ip),
     }

@@ -5,6 +5,7 @@
 // twiddle table, and picks the FFT frame.  The compute entry points only
 // enqueue work on the caller's stream (memset of atomically accumulated
 // outputs + one kernel) and allocate nothing.
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -37,7 +38,9 @@ struct EffPlan {
   int N;
   int K;
   int sy[2], off[2], E[2];
-  int threads;
+  int threads;   // per CTA when one CTA handles a patch
+  int threads2;  // per CTA of a 2-CTA cluster
+  int num_sms;
   int device;
   float2* win0;
   float2* win1;
@@ -48,6 +51,8 @@ namespace {
 
 thread_local std::string g_last_error;
 constexpr size_t kSmemLimit = 227u * 1024u;
+// 0: choose per call; 1: one CTA per patch; 2: a 2-CTA cluster per patch.
+std::atomic<int> g_cluster_mode{0};
 
 int fail(int code, const std::string& msg) {
   g_last_error = msg;
@@ -84,15 +89,26 @@ eff::Params base_params(const EffPlan* p) {
 }
 
 int run(const EffPlan* p, int op, const eff::Params& P, int batch, void* stream) {
-  const size_t smem = eff::smem_bytes(p->N, op, P, p->threads);
+  const size_t smem1 = eff::smem_bytes(p->N, op, P, p->threads, 1);
+  const size_t smem2 = eff::smem_bytes(p->N, op, P, p->threads2, 2);
+  // A 2-CTA cluster per patch when one CTA's frame does not fit, or when the
+  // doubled grid still fits in one wave (more SMs on a small launch).
+  const int mode = g_cluster_mode.load();
+  int CL;
+  if (smem1 > kSmemLimit) CL = 2;
+  else if (mode == 1) CL = 1;
+  else if (mode == 2) CL = 2;
+  else CL = (2LL * p->K * batch <= p->num_sms) ? 2 : 1;
+  const size_t smem = CL == 2 ? smem2 : smem1;
+  const int threads = CL == 2 ? p->threads2 : p->threads;
   if (smem > kSmemLimit)
     return fail(EFF_ERR_UNSUPPORTED, "frame needs " + std::to_string(smem) + " bytes of shared memory");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   cudaError_t e;
   switch (p->N) {
-    case 64: e = eff::launch_n64(op, P, p->K, batch, p->threads, smem, st); break;
-    case 128: e = eff::launch_n128(op, P, p->K, batch, p->threads, smem, st); break;
-    case 256: e = eff::launch_n256(op, P, p->K, batch, p->threads, smem, st); break;
+    case 64: e = eff::launch_n64(op, CL, P, p->K, batch, threads, smem, st); break;
+    case 128: e = eff::launch_n128(op, CL, P, p->K, batch, threads, smem, st); break;
+    case 256: e = eff::launch_n256(op, CL, P, p->K, batch, threads, smem, st); break;
     default: return fail(EFF_ERR_UNSUPPORTED, "frame size");
   }
   if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
@@ -235,16 +251,19 @@ int eff_plan_create(const EffGeom* geom, const float* win0, const float* win1, E
     for (;;) {
       size_t worst = 0;
       for (int op = 0; op < eff::kNumOps; ++op) {
-        const size_t s = eff::smem_bytes(p.N, op, P, p.threads);
+        const size_t s = eff::smem_bytes(p.N, op, P, p.threads, 1);
         if (s > worst) worst = s;
       }
-      if (worst <= kSmemLimit || p.threads <= 64) break;
+      if (worst <= kSmemLimit || p.threads <= 128) break;
       p.threads /= 2;
     }
+    p.threads2 = p.N >= 128 ? 256 : 128;
   }
 
   cudaError_t e = cudaGetDevice(&p.device);
   if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  e = cudaDeviceGetAttribute(&p.num_sms, cudaDevAttrMultiProcessorCount, p.device);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceGetAttribute");
 
   // Twiddle table [k1*G + g] = exp(-2 pi i g k1 / N), FP64 then rounded.
   const int G = p.N / 16;
@@ -462,6 +481,12 @@ int eff_mu_update(float* x, const float* num, const float* den, float tol, int r
   cudaError_t e = eff::launch_mu_update(x, num, den, tol, rows, cols, border0, border1, num_max_bits,
                                         floor_rel, xmax_bits, static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(e, "mu_update launch");
+  return EFF_OK;
+}
+
+int eff_set_cluster_mode(int mode) {
+  if (mode < 0 || mode > 2) return fail(EFF_ERR_INVALID, "cluster mode must be 0, 1 or 2");
+  g_cluster_mode.store(mode);
   return EFF_OK;
 }
 

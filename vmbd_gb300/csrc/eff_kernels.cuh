@@ -19,11 +19,19 @@
 //     fp32 atomics (forward: full-convolution extent, cropped by mode; image
 //     adjoint: windowed, patch extent) or stores the PSF gradient.
 //
+// With CL = 2 a patch is processed by a cluster of two CTAs: CTA c owns the
+// column units [c*N/4, (c+1)*N/4) of the half spectrum (CTA 0 also the N/2
+// bin) in its shared memory; the row passes write and read the peer's
+// columns through distributed shared memory, the column pass is local.
+//
 // Reference semantics: OlaGPU.cnv / OlaGPU.cnvtp, olaGPU.py:170-311.
 #pragma once
+#include <cooperative_groups.h>
+
 #include "eff_fft.cuh"
 
 namespace eff {
+namespace cg = cooperative_groups;
 
 enum Op : int {
   OP_SPEC_IMAGE = 0,  // X-hat of the windowed patches (OlaGPU X object, olaGPU.py:147-157)
@@ -59,7 +67,9 @@ struct Params {
   long long x_bs, f_bs, y_bs, spec_bs, out0_bs, out1_bs;  // per-image strides
 };
 
-__host__ __device__ constexpr int frame_pitch(int N) { return N / 2 + 1; }
+// Half-spectrum bins a CTA stores per row: all N/2+1 (CL = 1) or its
+// quarter plus, on CTA 0, the N/2 bin (CL = 2).
+__host__ __device__ constexpr int frame_pitch(int N, int CL = 1) { return CL == 1 ? N / 2 + 1 : N / 4 + 1; }
 __host__ __device__ constexpr int even_up(int v) { return (v + 1) & ~1; }
 // Threads per CTA the kernel is compiled for (the host may launch fewer).
 __host__ __device__ constexpr int max_threads(int N) { return N >= 256 ? 256 : 512; }
@@ -90,6 +100,28 @@ __device__ __forceinline__ unsigned group_mask(int lane) {
   constexpr int G = FftShape<N>::G;
   return G == 32 ? 0xffffffffu : (((1u << G) - 1u) << (lane & ~(G - 1)));
 }
+
+// The half-spectrum frame of one patch, possibly split over a cluster.
+template <int N, int CL>
+struct Frame {
+  static constexpr int HP = frame_pitch(N, CL);
+  static constexpr int Q = N / 4;
+  float2* part[CL];  // generic pointers to every CTA's frame (own one included)
+  float2* local;     // this CTA's frame (shared window)
+  int rank;
+  // Owner and local column of half-spectrum bin b.
+  __device__ __forceinline__ static int owner(int b) { return (CL == 1 || b < Q || b == N / 2) ? 0 : 1; }
+  __device__ __forceinline__ static int lcol(int b) {
+    return CL == 1 ? b : (b == N / 2 ? Q : (b < Q ? b : b - Q));
+  }
+  __device__ __forceinline__ float2* at(int row, int b) const {
+    return part[owner(b)] + row * HP + lcol(b);
+  }
+  // Local columns of column unit u (this CTA owns it): u's bin, and for the
+  // DC unit the N/2 bin.
+  __device__ __forceinline__ int col_of(int u) const { return CL == 1 ? u : u - rank * Q; }
+  static constexpr int kDcN = CL == 1 ? N / 2 : Q;
+};
 
 // Window weight ws[k=(m,n)][r][c] from the per-dim (alpha, gamma) tables:
 // alpha*alpha' inside the image, gamma*gamma' = 1/(patches covering the
@@ -145,46 +177,48 @@ __device__ __forceinline__ void load_rows(const Params& P, const Patch& T, int r
   }
 }
 
-// R2C of one pair of rows already in v (layout A) into frame rows
-// base+ra, base+ra+1.
-template <int N>
-__device__ __forceinline__ void r2c_store(float2 (&v)[16], float2* frame, int row, float2* scr,
+// R2C of one pair of rows already in v (layout A) into frame rows row,
+// row+1 (bins go to the CTA that owns their column).
+template <int N, int CL>
+__device__ __forceinline__ void r2c_store(float2 (&v)[16], const Frame<N, CL>& F, int row, float2* scr,
                                           const float2* tw, int g, unsigned gmask) {
   constexpr int G = FftShape<N>::G;
-  constexpr int HP = frame_pitch(N);
+  constexpr int HP = Frame<N, CL>::HP;
   fft_fwd<N>(v, g, scr, tw, gmask);
   float2 p[16];
   hermitian_partner<N>(v, p, g, gmask);
-  float2* rowa = frame + row * HP;
-  float2* rowb = rowa + HP;
 #pragma unroll
   for (int j = 0; j <= 8; ++j) {
     if (j == 8 && g != 0) break;
     const int kk = g + G * j;
-    rowa[kk] = make_float2(0.5f * (v[j].x + p[j].x), 0.5f * (v[j].y - p[j].y));
-    rowb[kk] = make_float2(0.5f * (v[j].y + p[j].y), 0.5f * (p[j].x - v[j].x));
+    // bins g + G*j: j < 4 (and the N/2 bin, j = 8) lie in the first quarter
+    float2* base = F.part[(CL == 1 || j < 4 || j == 8) ? 0 : CL - 1];
+    const int col = CL == 1 ? kk : (j == 8 ? Frame<N, CL>::Q : (j < 4 ? kk : kk - Frame<N, CL>::Q));
+    float2* rowa = base + row * HP + col;
+    rowa[0] = make_float2(0.5f * (v[j].x + p[j].x), 0.5f * (v[j].y - p[j].y));
+    rowa[HP] = make_float2(0.5f * (v[j].y + p[j].y), 0.5f * (p[j].x - v[j].x));
   }
 }
 
 // C2R of frame rows (ra, ra+1); returns real row ra in .x, ra+1 in .y,
 // layout A (register m holds column g + G*m).
-template <int N>
-__device__ __forceinline__ void c2r_unit(const float2* frame, int ra, float2 (&v)[16], float2* scr,
+template <int N, int CL>
+__device__ __forceinline__ void c2r_unit(const Frame<N, CL>& F, int ra, float2 (&v)[16], float2* scr,
                                          const float2* tw, int g, unsigned gmask) {
   constexpr int G = FftShape<N>::G;
-  constexpr int HP = frame_pitch(N);
-  const float2* rowa = frame + ra * HP;
-  const float2* rowb = rowa + HP;
+  constexpr int HP = Frame<N, CL>::HP;
 #pragma unroll
   for (int j = 0; j < 16; ++j) {
     const int kk = g + G * j;
     float2 ya, yb;
     if (j < 8 || (j == 8 && g == 0)) {
-      ya = rowa[kk];
-      yb = rowb[kk];
+      const float2* pa = F.at(ra, kk);
+      ya = pa[0];
+      yb = pa[HP];
     } else {
-      ya = rowa[N - kk];
-      yb = rowb[N - kk];
+      const float2* pa = F.at(ra, N - kk);
+      ya = pa[0];
+      yb = pa[HP];
       ya.y = -ya.y;
       yb.y = -yb.y;
     }
@@ -193,41 +227,40 @@ __device__ __forceinline__ void c2r_unit(const float2* frame, int ra, float2 (&v
   fft_inv<N>(v, g, scr, tw, gmask);
 }
 
-// Column u (u == 0: columns 0 and N/2 packed as re/im) of rows [base, base+rows).
-template <int N>
-__device__ __forceinline__ void load_column(const float2* frame, int u, int base, int rows, int g,
-                                            float2 (&v)[16]) {
+// Local column `col` (dc: local columns 0 and dcN packed as re/im) of rows
+// [base, base+rows), frame pitch HP.
+template <int N, int HP>
+__device__ __forceinline__ void load_column(const float2* frame, int col, bool dc, int dcN, int base, int rows,
+                                            int g, float2 (&v)[16]) {
   constexpr int G = FftShape<N>::G;
-  constexpr int HP = frame_pitch(N);
 #pragma unroll
   for (int mm = 0; mm < 16; ++mm) {
     const int r = g + G * mm;
     if (r < rows) {
       const float2* row = frame + (base + r) * HP;
-      v[mm] = (u == 0) ? make_float2(row[0].x, row[N / 2].x) : row[u];
+      v[mm] = dc ? make_float2(row[0].x, row[dcN].x) : row[col];
     } else {
       v[mm] = make_float2(0.f, 0.f);
     }
   }
 }
 
-// Inverse-transformed column u to rows [base, base + even(rows)).
-template <int N>
-__device__ __forceinline__ void store_column(float2* frame, int u, int base, int rows, int g,
-                                             const float2 (&v)[16]) {
+// Inverse-transformed column to rows [base, base + even(rows)).
+template <int N, int HP>
+__device__ __forceinline__ void store_column(float2* frame, int col, bool dc, int dcN, int base, int rows,
+                                             int g, const float2 (&v)[16]) {
   constexpr int G = FftShape<N>::G;
-  constexpr int HP = frame_pitch(N);
   const int rows_e = even_up(rows);
 #pragma unroll
   for (int mm = 0; mm < 16; ++mm) {
     const int r = g + G * mm;
     if (r < rows_e) {
       float2* row = frame + (base + r) * HP;
-      if (u == 0) {
+      if (dc) {
         row[0] = make_float2(v[mm].x, 0.f);
-        row[N / 2] = make_float2(v[mm].y, 0.f);
+        row[dcN] = make_float2(v[mm].y, 0.f);
       } else {
-        row[u] = v[mm];
+        row[col] = v[mm];
       }
     }
   }
@@ -236,11 +269,11 @@ __device__ __forceinline__ void store_column(float2* frame, int u, int base, int
 // Column spectrum of a real-row-transformed operand.  u != 0: a[] is the
 // spectrum of column u.  u == 0: the packed transform of columns 0 and N/2 is
 // split into a[] (column 0) and b[] (column N/2).
-template <int N>
-__device__ __forceinline__ void column_spectrum(const float2* frame, int u, int base, int rows,
-                                                int g, float2* scr, const float2* tw,
+template <int N, int HP>
+__device__ __forceinline__ void column_spectrum(const float2* frame, int u, int col, int dcN, int base,
+                                                int rows, int g, float2* scr, const float2* tw,
                                                 unsigned gmask, float2 (&a)[16], float2 (&b)[16]) {
-  load_column<N>(frame, u, base, rows, g, a);
+  load_column<N, HP>(frame, col, u == 0, dcN, base, rows, g, a);
   fft_fwd<N>(a, g, scr, tw, gmask);
   if (u == 0) {
     float2 p[16];
@@ -299,23 +332,23 @@ __device__ __forceinline__ void column_product(const float2 (&a)[16], const floa
 // Column 0 of the image and column 0 of the PSFs share one complex transform
 // (then column N/2 of both); the two products are packed as
 // col0 + i*colN for one inverse transform.
-template <int N>
-__device__ __forceinline__ void fwd_both_dc(float2* frame, int rowsA, int baseB, int rowsB, int E0,
+template <int N, int HP>
+__device__ __forceinline__ void fwd_both_dc(float2* frame, int dcN, int rowsA, int baseB, int rowsB, int E0,
                                             int g, float2* scr, const float2* tw, unsigned gmask,
                                             float scale, float2* a_out, float2* b_out) {
   constexpr int G = FftShape<N>::G;
-  constexpr int HP = frame_pitch(N);
   float2 prod[16];
 #pragma unroll 1
   for (int half = 0; half < 2; ++half) {
-    const int col = half ? N / 2 : 0;
+    const int lcol = half ? dcN : 0;     // local column in the frame
+    const int col = half ? N / 2 : 0;    // bin (spectrum layout)
     float2 v[16];
     float amax = 0.f, bmax = 0.f;
 #pragma unroll
     for (int mm = 0; mm < 16; ++mm) {
       const int r = g + G * mm;
-      v[mm] = make_float2(r < rowsA ? frame[r * HP + col].x : 0.f,
-                          r < rowsB ? frame[(baseB + r) * HP + col].x : 0.f);
+      v[mm] = make_float2(r < rowsA ? frame[r * HP + lcol].x : 0.f,
+                          r < rowsB ? frame[(baseB + r) * HP + lcol].x : 0.f);
       amax = fmaxf(amax, fabsf(v[mm].x));
       bmax = fmaxf(bmax, fabsf(v[mm].y));
     }
@@ -346,23 +379,42 @@ __device__ __forceinline__ void fwd_both_dc(float2* frame, int rowsA, int baseB,
     }
   }
   fft_inv<N>(prod, g, scr, tw, gmask);
-  store_column<N>(frame, 0, 0, E0, g, prod);
+  store_column<N, HP>(frame, 0, true, dcN, 0, E0, g, prod);
 }
 
-template <int N, int OP>
+template <int N, int OP, int CL>
 __global__ void __launch_bounds__(max_threads(N)) eff_kernel(Params P) {
   constexpr int G = FftShape<N>::G;
   constexpr int A = opnd_a(OP);
+  constexpr int HP = frame_pitch(N, CL);
   extern __shared__ __align__(16) float2 smem[];
   float2* tw = smem;         // N entries
-  float2* frame = smem + N;  // frame_rows(P, OP) * (N/2+1)
+  float2* frame = smem + N;  // frame_rows(P, OP) * HP
   const int tid = threadIdx.x;
   const int NG = blockDim.x / G;
   const int gid = tid / G, g = tid % G;
   const unsigned gmask = group_mask<N>(tid & 31);
 
+  Frame<N, CL> F;
+  F.local = frame;
+  if constexpr (CL == 1) {
+    F.rank = 0;
+    F.part[0] = frame;
+  } else {
+    cg::cluster_group cluster = cg::this_cluster();
+    F.rank = (int)cluster.block_rank();
+#pragma unroll
+    for (int r = 0; r < CL; ++r) F.part[r] = cluster.map_shared_rank(frame, r);
+  }
+  auto phase_sync = [&]() {
+    if constexpr (CL == 1) __syncthreads();
+    else cg::this_cluster().sync();
+  };
+  // Workers across the cluster for the row passes.
+  const int wid = F.rank * NG + gid, NW = CL * NG;
+
   Patch T;
-  T.k = blockIdx.x;
+  T.k = blockIdx.x / CL;
   T.m = T.k / P.csf1;
   T.n = T.k - T.m * P.csf1;
   const long long b = blockIdx.y;
@@ -380,7 +432,7 @@ __global__ void __launch_bounds__(max_threads(N)) eff_kernel(Params P) {
 
   const int rowsA = opnd_rows(P, A);
   const int baseB = even_up(rowsA);
-  float2* scr = frame + frame_rows(P, OP) * frame_pitch(N) + gid * FftShape<N>::SCR;
+  float2* scr = frame + frame_rows(P, OP) * HP + gid * FftShape<N>::SCR;
 
   for (int i = tid; i < N; i += blockDim.x) tw[i] = __ldg(P.tw + i);
 
@@ -389,7 +441,7 @@ __global__ void __launch_bounds__(max_threads(N)) eff_kernel(Params P) {
     if (P.loss && T.y_obs) {
       const long long npx = (long long)P.sy0 * P.sy1;
       const long long chunk = (npx + gridDim.x - 1) / gridDim.x;
-      const long long p0 = T.k * chunk;
+      const long long p0 = blockIdx.x * chunk;
       const long long p1 = min(npx, p0 + chunk);
       float acc = 0.f;
       for (long long p = p0 + tid; p < p1; p += blockDim.x) {
@@ -402,13 +454,14 @@ __global__ void __launch_bounds__(max_threads(N)) eff_kernel(Params P) {
       if ((tid & 31) == 0) atomicAdd(P.loss + b, 0.5 * d);
     }
   }
-  __syncthreads();
+  // The peer must not write into this CTA's frame before it is running.
+  phase_sync();
 
   // Phase 1: row transforms of operand A (and B).
   {
     const int nA = (rowsA + 1) >> 1;
     const int nB = has_b(OP) ? (P.sf0 + 1) >> 1 : 0;
-    for (int u = gid; u < nA + nB; u += NG) {
+    for (int u = wid; u < nA + nB; u += NW) {
       float2 v[16];
       int row;
       if (u < nA) {
@@ -418,22 +471,26 @@ __global__ void __launch_bounds__(max_threads(N)) eff_kernel(Params P) {
         load_rows<N, OPND_PSF>(P, T, 2 * (u - nA), g, v);
         row = baseB + 2 * (u - nA);
       }
-      r2c_store<N>(v, frame, row, scr, tw, g, gmask);
+      r2c_store<N, CL>(v, F, row, scr, tw, g, gmask);
     }
   }
-  __syncthreads();
+  phase_sync();
 
-  // Phase 2: column transforms, products, inverse column transforms.
+  // Phase 2: column transforms, products, inverse column transforms (local).
+  constexpr int kUnits = N / 2 / CL;  // column units this CTA owns
+  constexpr int dcN = Frame<N, CL>::kDcN;
   const float scale = 1.f / (float(N) * float(N));
-  for (int u = gid; u < N / 2; u += NG) {
+  for (int lu = gid; lu < kUnits; lu += NG) {
+    const int u = F.rank * kUnits + lu;
+    const int col = lu;
     if constexpr (OP == OP_FWD_BOTH) {
       if (u == 0) {
-        fwd_both_dc<N>(frame, rowsA, baseB, P.sf0, P.E0, g, scr, tw, gmask, scale, a_out, b_out);
+        fwd_both_dc<N, HP>(frame, dcN, rowsA, baseB, P.sf0, P.E0, g, scr, tw, gmask, scale, a_out, b_out);
         continue;
       }
     }
     float2 a[16], ab[16];
-    column_spectrum<N>(frame, u, 0, rowsA, g, scr, tw, gmask, a, ab);
+    column_spectrum<N, HP>(frame, u, col, dcN, 0, rowsA, g, scr, tw, gmask, a, ab);
     if constexpr (OP == OP_SPEC_IMAGE || OP == OP_SPEC_PSF) {
       store_spectrum<N>(a_out, u, g, a, ab);
     } else if constexpr (OP == OP_FWD_IMAGE || OP == OP_FWD_PSF) {
@@ -441,19 +498,19 @@ __global__ void __launch_bounds__(max_threads(N)) eff_kernel(Params P) {
       float2 pr[16];
       column_product<N, false>(a, ab, b0, u, g, scale, pr);
       fft_inv<N>(pr, g, scr, tw, gmask);
-      store_column<N>(frame, u, 0, P.E0, g, pr);
+      store_column<N, HP>(frame, col, u == 0, dcN, 0, P.E0, g, pr);
     } else if constexpr (OP == OP_FWD_BOTH) {
       // u != 0 here: a holds the image column spectrum; transform the PSF
       // column through the same code and multiply in place
       if (a_out) store_spectrum<N>(a_out, u, g, a, ab);
       float2 s[16];
-      load_column<N>(frame, u, baseB, P.sf0, g, s);
+      load_column<N, HP>(frame, col, false, dcN, baseB, P.sf0, g, s);
       fft_fwd<N>(s, g, scr, tw, gmask);
       if (b_out) store_spectrum<N>(b_out, u, g, s, s);
 #pragma unroll
       for (int j = 0; j < 16; ++j) a[j] = cscale(cmul(a[j], s[j]), scale);
       fft_inv<N>(a, g, scr, tw, gmask);
-      store_column<N>(frame, u, 0, P.E0, g, a);
+      store_column<N, HP>(frame, col, false, dcN, 0, P.E0, g, a);
     } else {
       // adjoints: output 0 = image (conj F-hat, rows sw0), 1 = PSF (conj X-hat, rows sf0)
 #pragma unroll 1
@@ -463,21 +520,23 @@ __global__ void __launch_bounds__(max_threads(N)) eff_kernel(Params P) {
         column_product<N, true>(a, ab, o == 0 ? b0 : b1, u, g, scale, pr);
         fft_inv<N>(pr, g, scr, tw, gmask);
         const int base = (o == 1 && P.out0) ? even_up(P.sw0) : 0;
-        store_column<N>(frame, u, base, o == 0 ? P.sw0 : P.sf0, g, pr);
+        store_column<N, HP>(frame, col, u == 0, dcN, base, o == 0 ? P.sw0 : P.sf0, g, pr);
       }
     }
   }
+  // Spectrum kernels are done: every remote access (phase 1) precedes the
+  // last cluster barrier, so a CTA may leave while its peer still works.
   if constexpr (OP == OP_SPEC_IMAGE || OP == OP_SPEC_PSF) return;
-  __syncthreads();
+  phase_sync();
 
   // Phase 3: inverse row transforms and epilogues.
   if constexpr (OP == OP_FWD_IMAGE || OP == OP_FWD_PSF || OP == OP_FWD_BOTH) {
     float* out = P.out0 + b * P.out0_bs;
     const int i0 = T.m * P.hop0 - P.off0, j0 = T.n * P.hop1 - P.off1;
     const int nu = (P.E0 + 1) >> 1;
-    for (int u = gid; u < nu; u += NG) {
+    for (int u = wid; u < nu; u += NW) {
       float2 v[16];
-      c2r_unit<N>(frame, 2 * u, v, scr, tw, g, gmask);
+      c2r_unit<N, CL>(F, 2 * u, v, scr, tw, g, gmask);
       const int ia = i0 + 2 * u;
       const bool rb = 2 * u + 1 < P.E0;
 #pragma unroll
@@ -493,11 +552,11 @@ __global__ void __launch_bounds__(max_threads(N)) eff_kernel(Params P) {
     const int n0 = P.out0 ? (P.sw0 + 1) >> 1 : 0;
     const int n1 = P.out1 ? (P.sf0 + 1) >> 1 : 0;
     const int base1 = P.out0 ? even_up(P.sw0) : 0;
-    for (int u = gid; u < n0 + n1; u += NG) {
+    for (int u = wid; u < n0 + n1; u += NW) {
       const bool img = u < n0;
       const int r = img ? 2 * u : 2 * (u - n0);
       float2 v[16];
-      c2r_unit<N>(frame, img ? r : base1 + r, v, scr, tw, g, gmask);
+      c2r_unit<N, CL>(F, img ? r : base1 + r, v, scr, tw, g, gmask);
       if (img) {
         // image gradient: window, overlap-add into gx
         float* out = P.out0 + b * P.out0_bs;
@@ -530,6 +589,8 @@ __global__ void __launch_bounds__(max_threads(N)) eff_kernel(Params P) {
       }
     }
   }
+  // Peers read this CTA's frame in phase 3: stay resident until they finish.
+  if constexpr (CL > 1) phase_sync();
 }
 
 }  // namespace eff

@@ -5,44 +5,70 @@
 
 namespace eff {
 
-// Shared-memory bytes of one CTA: twiddles + frame + per-group exchange scratch.
-inline size_t smem_bytes(int N, int op, const Params& P, int threads) {
+// Shared-memory bytes of one CTA: twiddles + frame (its share of the columns)
+// + per-group exchange scratch.
+inline size_t smem_bytes(int N, int op, const Params& P, int threads, int CL) {
   const int G = N / 16;
   const int scr = 16 * (G + 1) + 8;
-  return sizeof(float2) * ((size_t)N + (size_t)frame_rows(P, op) * frame_pitch(N) +
+  return sizeof(float2) * ((size_t)N + (size_t)frame_rows(P, op) * frame_pitch(N, CL) +
                            (size_t)(threads / G) * scr);
 }
 
-template <int N, int OP>
+template <int N, int OP, int CL>
 cudaError_t launch_one(const Params& P, int K, int batch, int threads, size_t smem, cudaStream_t st) {
   static std::atomic<int> attr_bytes[64];
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
+  auto kern = eff_kernel<N, OP, CL>;
   if (dev >= 64 || attr_bytes[dev].load() < (int)smem) {
-    e = cudaFuncSetAttribute(eff_kernel<N, OP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     if (dev < 64) attr_bytes[dev].store((int)smem);
   }
-  eff_kernel<N, OP><<<dim3(K, batch), threads, smem, st>>>(P);
+  if constexpr (CL == 1) {
+    kern<<<dim3(K, batch), threads, smem, st>>>(P);
+  } else {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(K * CL, batch);
+    cfg.blockDim = dim3(threads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = CL;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    e = cudaLaunchKernelEx(&cfg, kern, P);
+    if (e != cudaSuccess) return e;
+  }
   return cudaGetLastError();
 }
 
-template <int N>
-cudaError_t launch_n(int op, const Params& P, int K, int batch, int threads, size_t smem, cudaStream_t st) {
+template <int N, int CL>
+cudaError_t launch_ncl(int op, const Params& P, int K, int batch, int threads, size_t smem, cudaStream_t st) {
   switch (op) {
-    case OP_SPEC_IMAGE: return launch_one<N, OP_SPEC_IMAGE>(P, K, batch, threads, smem, st);
-    case OP_SPEC_PSF: return launch_one<N, OP_SPEC_PSF>(P, K, batch, threads, smem, st);
-    case OP_FWD_IMAGE: return launch_one<N, OP_FWD_IMAGE>(P, K, batch, threads, smem, st);
-    case OP_FWD_PSF: return launch_one<N, OP_FWD_PSF>(P, K, batch, threads, smem, st);
-    case OP_FWD_BOTH: return launch_one<N, OP_FWD_BOTH>(P, K, batch, threads, smem, st);
-    case OP_ADJ: return launch_one<N, OP_ADJ>(P, K, batch, threads, smem, st);
+    case OP_SPEC_IMAGE: return launch_one<N, OP_SPEC_IMAGE, CL>(P, K, batch, threads, smem, st);
+    case OP_SPEC_PSF: return launch_one<N, OP_SPEC_PSF, CL>(P, K, batch, threads, smem, st);
+    case OP_FWD_IMAGE: return launch_one<N, OP_FWD_IMAGE, CL>(P, K, batch, threads, smem, st);
+    case OP_FWD_PSF: return launch_one<N, OP_FWD_PSF, CL>(P, K, batch, threads, smem, st);
+    case OP_FWD_BOTH: return launch_one<N, OP_FWD_BOTH, CL>(P, K, batch, threads, smem, st);
+    case OP_ADJ: return launch_one<N, OP_ADJ, CL>(P, K, batch, threads, smem, st);
     default: return cudaErrorInvalidValue;
   }
 }
 
-cudaError_t launch_n64(int op, const Params& P, int K, int batch, int threads, size_t smem, cudaStream_t st);
-cudaError_t launch_n128(int op, const Params& P, int K, int batch, int threads, size_t smem, cudaStream_t st);
-cudaError_t launch_n256(int op, const Params& P, int K, int batch, int threads, size_t smem, cudaStream_t st);
+template <int N>
+cudaError_t launch_n(int op, int CL, const Params& P, int K, int batch, int threads, size_t smem,
+                     cudaStream_t st) {
+  return CL == 2 ? launch_ncl<N, 2>(op, P, K, batch, threads, smem, st)
+                 : launch_ncl<N, 1>(op, P, K, batch, threads, smem, st);
+}
+
+cudaError_t launch_n64(int op, int CL, const Params& P, int K, int batch, int threads, size_t smem, cudaStream_t st);
+cudaError_t launch_n128(int op, int CL, const Params& P, int K, int batch, int threads, size_t smem, cudaStream_t st);
+cudaError_t launch_n256(int op, int CL, const Params& P, int K, int batch, int threads, size_t smem, cudaStream_t st);
 
 }  // namespace eff
