@@ -52,6 +52,11 @@ FLUSH_BYTES = 256 << 20
 # steps with edgetaper.  Latent image 536x536 (valid mode), win2winaux patches
 # 120x120 (hop 60), frame 256.
 MFBD = dict(sy=(512, 512), sf=(25, 25), csf=(8, 8), frames=100, n_pg=10, n_mu=5)
+# Uneven batch: 64 images in one persistent launch per direction: 24 at
+# 256x256 (4x4 grid, 15x15 Gaussian PSFs), 24 at 384x512 (6x8, 21x21 motion),
+# 16 at 1024x1024 (12x12, 31x31 motion); win2winaux geometry per class.
+CFG4 = [((256, 256), (4, 4), (15, 15), "gauss", 24), ((384, 512), (6, 8), (21, 21), "motion", 24),
+        ((1024, 1024), (12, 12), (31, 31), "motion", 16)]
 
 
 def peaks():
@@ -394,6 +399,41 @@ def run_mfbd(args, dev, n_timed, with_unfused=True):
     return out
 
 
+def run_cfg4(args, dev, n_timed):
+    """Images/s of the loss/gradient step over the uneven 64-image batch with
+    the autotuner's strategy (every candidate's time is reported)."""
+    import torch
+    from vmbd_gb300 import autotune, geometry, synth
+    from vmbd_gb300.eff import EffPlan
+    plans, counts, xs, fs, yo = [], [], [], [], []
+    for ci, (sx, csf, sf, kind, count) in enumerate(CFG4):
+        wa = geometry.win2winaux(sx, csf, 0.5)
+        plan = EffPlan(wa, sf, "valid", device=dev)
+        gen = synth.motion_psfs if kind == "motion" else synth.gaussian_psfs
+        # 4 distinct seeded images / PSF sets per class, repeated to the count
+        xu = np.stack([synth.blob_edge_image(sx, seed=100 * ci + i) for i in range(4)])
+        fu = np.stack([gen(wa.K, sf, seed=100 * ci + 50 + i) for i in range(4)])
+        x = torch.from_numpy(xu[np.arange(count) % 4]).to(dev)
+        f = torch.from_numpy(fu[np.arange(count) % 4]).to(dev)
+        y = plan.forward_both(x, f)
+        y += 0.01 * torch.randn(y.shape, device=dev, generator=torch.Generator(device=dev).manual_seed(ci))
+        plans.append(plan)
+        counts.append(count)
+        xs.append(x)
+        fs.append(f)
+        yo.append(y)
+    best, times = autotune.tune(plans, counts, xs, fs, yo)
+    runner = autotune.BatchRunner(plans, counts, best)
+    ms, _, _ = autotune.time_step(runner, xs, fs, yo, reps=max(3, n_timed), warmup=args.warmup)
+    n_img = sum(counts)
+    items = sum(p.K * c for p, c in zip(plans, counts))
+    return {"value": n_img / (ms * 1e-3), "unit": "images/s", "ms_per_step": ms, "strategy": best,
+            "candidates_ms": {k: v for k, v in times.items() if not k.endswith(":error")},
+            "patches_per_step": items, "frames": [p.N for p in plans],
+            "config": "64 images: 24 x 256^2 (4x4, 15^2 Gaussian), 24 x 384x512 (6x8, 21^2 motion), "
+                      "16 x 1024^2 (12x12, 31^2 motion); loss + both gradients per step"}
+
+
 def barrier(world):
     if world > 1:
         import torch.distributed as dist
@@ -545,6 +585,10 @@ def main():
             line["mfbd"] = run_mfbd(args, dev, n_timed=20)
         except Exception as e:  # reported, not fatal to the headline line
             line["mfbd"] = {"error": repr(e)[:300]}
+        try:
+            line["cfg4_batch"] = run_cfg4(args, dev, n_timed=10)
+        except Exception as e:
+            line["cfg4_batch"] = {"error": repr(e)[:300]}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         r_gpu = R["y"].astype(np.float64) - R["y_obs"]
         t_cpu, reps, cores, (y_o, gx_o, gf_o) = cpu_sample(w, wa, R["x_np"], R["f_np"], R["y_obs"], r_gpu)

@@ -191,6 +191,27 @@ int eff_mu_update(float* x, const float* num, const float* den, float tol, int r
                   int border1, const unsigned* num_max_bits, float floor_rel, unsigned* xmax_bits,
                   void* stream);
 
+/* Uneven batches in one persistent launch (BASELINE's batched workload):
+ * images of up to 8 geometries (one plan each, counts[c] images of plan c,
+ * stored back to back per class) are processed by one kernel launch per
+ * direction.  The batch keeps a device work list of (class, image, patch)
+ * items, largest FFT frame first, walked statically by a grid of 2-CTA
+ * clusters (one CTA per SM).  Per-class arguments are arrays of n_classes
+ * device pointers (host arrays); outputs accumulated with atomics (y, gx,
+ * loss) are cleared by the call. */
+typedef struct EffBatch EffBatch;
+int eff_batch_create(const EffPlan* const* plans, const int* counts, int n_classes, EffBatch** batch);
+int eff_batch_destroy(EffBatch* batch);
+int eff_batch_items(const EffBatch* batch);
+/* eff_forward_both over the batch: x, f -> y (+ both spectra, nullable). */
+int eff_batch_forward_both(const EffBatch* batch, const float* const* x, const float* const* f, float* const* y,
+                           void* const* xhat_out, void* const* fhat_out, void* stream);
+/* eff_adjoint_residual over the batch (y_obs and loss nullable: plain
+ * adjoint of y); gx needs fhat, gf needs xhat. */
+int eff_batch_adjoint_residual(const EffBatch* batch, const float* const* y, const float* const* y_obs,
+                               const void* const* fhat, const void* const* xhat, float* const* gx,
+                               float* const* gf, double* const* loss, void* stream);
+
 /* How many CTAs process one patch, for all plans of the process:
  * 0 (default) per call -- a 2-CTA thread-block cluster when one CTA's frame
  * does not fit in shared memory or when twice the grid still fits on the

@@ -29,7 +29,8 @@ EXPORTS = (
     "eff_forward_both", "eff_adjoint_residual", "eff_loss_grad_workspace_bytes", "eff_loss_grad",
     "eff_static_scratch_bytes", "eff_loss_grad_static", "eff_edgetaper",
     "eff_adjoint_masked", "eff_dots3", "eff_pg_step", "eff_mu_update", "eff_max_nonneg",
-    "eff_set_cluster_mode",
+    "eff_set_cluster_mode", "eff_batch_create", "eff_batch_destroy", "eff_batch_items",
+    "eff_batch_forward_both", "eff_batch_adjoint_residual",
 )
 
 
@@ -87,6 +88,11 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "eff_pg_step": ([fp, fp, fp, fp, ip, ip, vp, ip, fp, vp], ip),
         "eff_max_nonneg": ([fp, ctypes.c_longlong, vp, vp], ip),
         "eff_set_cluster_mode": ([ip], ip),
+        "eff_batch_create": ([vp, vp, ip, ctypes.POINTER(vp)], ip),
+        "eff_batch_destroy": ([vp], ip),
+        "eff_batch_items": ([vp], ip),
+        "eff_batch_forward_both": ([vp, vp, vp, vp, vp, vp, vp], ip),
+        "eff_batch_adjoint_residual": ([vp, vp, vp, vp, vp, vp, vp, vp, vp], ip),
         "eff_mu_update": ([fp, fp, fp, ctypes.c_float, ip, ip, ip, ip, vp, ctypes.c_float, vp, vp], ip),
         "eff_loss_grad_static": ([vp, fp, fp, fp, vp, fp, fp, ip, vp], ip),
     }

@@ -18,6 +18,8 @@
 #include "../../include/vmbd_eff.h"
 
 namespace eff {
+int plan_params(const EffPlan* plan, Params* P, int* N);
+int plan_patches(const EffPlan* plan);
 cudaError_t launch_project(float* f, int K, int n, int mode, cudaStream_t st);
 cudaError_t launch_basis_project(const float* fs, const float* basis, float* w, int nb, int n,
                                  cudaStream_t st);
@@ -199,6 +201,15 @@ int loss_grad_impl(const EffPlan* plan, const float* x, const float* f, const fl
 }  // namespace
 
 int eff::set_error(int code, const std::string& msg) { return fail(code, msg); }
+
+int eff::plan_params(const EffPlan* plan, eff::Params* P, int* N) {
+  if (!plan) return fail(EFF_ERR_INVALID, "null plan");
+  *P = base_params(plan);
+  *N = plan->N;
+  return EFF_OK;
+}
+
+int eff::plan_patches(const EffPlan* plan) { return plan ? plan->K : 0; }
 
 extern "C" {
 

@@ -382,12 +382,16 @@ __device__ __forceinline__ void fwd_both_dc(float2* frame, int dcN, int rowsA, i
   store_column<N, HP>(frame, 0, true, dcN, 0, E0, g, prod);
 }
 
+// One patch `k` of image `b` through the three phases, on this CTA (and its
+// cluster peer when CL = 2).  `cta` / `ncta` number this CTA among the
+// CTAs that work on image b (for the loss share).  Every thread of the CTA
+// (and of the peer) must call it with the same arguments.
 template <int N, int OP, int CL>
-__global__ void __launch_bounds__(max_threads(N)) eff_kernel(Params P) {
+__device__ __forceinline__ void eff_patch(const Params& P, int k, long long b, float2* smem, int cta,
+                                          int ncta) {
   constexpr int G = FftShape<N>::G;
   constexpr int A = opnd_a(OP);
   constexpr int HP = frame_pitch(N, CL);
-  extern __shared__ __align__(16) float2 smem[];
   float2* tw = smem;         // N entries
   float2* frame = smem + N;  // frame_rows(P, OP) * HP
   const int tid = threadIdx.x;
@@ -414,10 +418,9 @@ __global__ void __launch_bounds__(max_threads(N)) eff_kernel(Params P) {
   const int wid = F.rank * NG + gid, NW = CL * NG;
 
   Patch T;
-  T.k = blockIdx.x / CL;
+  T.k = k;
   T.m = T.k / P.csf1;
   T.n = T.k - T.m * P.csf1;
-  const long long b = blockIdx.y;
   T.x = P.x ? P.x + b * P.x_bs : nullptr;
   T.f = P.f ? P.f + b * P.f_bs : nullptr;
   T.y = P.y ? P.y + b * P.y_bs : nullptr;
@@ -440,8 +443,8 @@ __global__ void __launch_bounds__(max_threads(N)) eff_kernel(Params P) {
   if constexpr (OP == OP_ADJ) {
     if (P.loss && T.y_obs) {
       const long long npx = (long long)P.sy0 * P.sy1;
-      const long long chunk = (npx + gridDim.x - 1) / gridDim.x;
-      const long long p0 = blockIdx.x * chunk;
+      const long long chunk = (npx + ncta - 1) / ncta;
+      const long long p0 = (long long)cta * chunk;
       const long long p1 = min(npx, p0 + chunk);
       float acc = 0.f;
       for (long long p = p0 + tid; p < p1; p += blockDim.x) {
@@ -454,7 +457,8 @@ __global__ void __launch_bounds__(max_threads(N)) eff_kernel(Params P) {
       if ((tid & 31) == 0) atomicAdd(P.loss + b, 0.5 * d);
     }
   }
-  // The peer must not write into this CTA's frame before it is running.
+  // The peer must not write into this CTA's frame before it is running (and,
+  // in a persistent loop, before this CTA has finished the previous patch).
   phase_sync();
 
   // Phase 1: row transforms of operand A (and B).
@@ -524,9 +528,12 @@ __global__ void __launch_bounds__(max_threads(N)) eff_kernel(Params P) {
       }
     }
   }
-  // Spectrum kernels are done: every remote access (phase 1) precedes the
-  // last cluster barrier, so a CTA may leave while its peer still works.
-  if constexpr (OP == OP_SPEC_IMAGE || OP == OP_SPEC_PSF) return;
+  // Spectrum kernels are done; with a cluster, wait for the peer's local
+  // column pass so that a following patch cannot write into its frame early.
+  if constexpr (OP == OP_SPEC_IMAGE || OP == OP_SPEC_PSF) {
+    if constexpr (CL > 1) phase_sync();
+    return;
+  }
   phase_sync();
 
   // Phase 3: inverse row transforms and epilogues.
@@ -591,6 +598,13 @@ __global__ void __launch_bounds__(max_threads(N)) eff_kernel(Params P) {
   }
   // Peers read this CTA's frame in phase 3: stay resident until they finish.
   if constexpr (CL > 1) phase_sync();
+}
+
+// One patch per CTA (CL = 1) or per 2-CTA cluster, images along blockIdx.y.
+template <int N, int OP, int CL>
+__global__ void __launch_bounds__(max_threads(N)) eff_kernel(Params P) {
+  extern __shared__ __align__(16) float2 smem[];
+  eff_patch<N, OP, CL>(P, blockIdx.x / CL, blockIdx.y, smem, blockIdx.x, gridDim.x);
 }
 
 }  // namespace eff

@@ -272,3 +272,86 @@ def basis_project(fs: torch.Tensor, basis: torch.Tensor) -> torch.Tensor:
     with torch.cuda.device(fs.device):
         _lib.check(lib.eff_basis_project(_ptr(fs), _ptr(basis), _ptr(w), nb, n, _stream(fs.device)))
     return w
+
+
+class EffBatch:
+    """Uneven batch over several plans in one persistent launch per direction
+    (``eff_batch_*``).  Per class c, arrays carry a leading dim of
+    ``counts[c]`` images."""
+
+    def __init__(self, plans, counts):
+        if len(plans) != len(counts) or not plans:
+            raise ValueError("one count per plan")
+        self.lib = _lib.load()
+        self.plans = list(plans)
+        self.counts = [int(c) for c in counts]
+        self.device = plans[0].device
+        n = len(plans)
+        arr = (ctypes.c_void_p * n)(*[p._h.value for p in plans])
+        cnt = (ctypes.c_int * n)(*self.counts)
+        h = ctypes.c_void_p()
+        with torch.cuda.device(self.device):
+            _lib.check(self.lib.eff_batch_create(arr, cnt, n, ctypes.byref(h)))
+        self._h = h
+        self._work = None
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                self.lib.eff_batch_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    @property
+    def items(self) -> int:
+        return self.lib.eff_batch_items(self._h)
+
+    @staticmethod
+    def _ptrs(ts):
+        if ts is None:
+            return None
+        return (ctypes.c_void_p * len(ts))(*[t.data_ptr() if t is not None else None for t in ts])
+
+    def _shapes(self, ts, shape_of, name):
+        for p, c, t in zip(self.plans, self.counts, ts):
+            want = (c,) + shape_of(p)
+            if tuple(t.shape) != want or t.dtype != torch.float32 or not t.is_contiguous() or not t.is_cuda:
+                raise IOError(f"{name}: expected contiguous float32 CUDA tensor {want}, got {tuple(t.shape)}")
+
+    def forward_both(self, xs, fs, ys=None, xhats=None, fhats=None):
+        self._shapes(xs, lambda p: p.sx, "x")
+        self._shapes(fs, lambda p: (p.K,) + p.sf, "f")
+        if ys is None:
+            ys = [torch.empty((c,) + p.sy, device=self.device) for p, c in zip(self.plans, self.counts)]
+        _lib.check(self.lib.eff_batch_forward_both(self._h, self._ptrs(xs), self._ptrs(fs), self._ptrs(ys),
+                                                   self._ptrs(xhats), self._ptrs(fhats), _stream(self.device)))
+        return ys
+
+    def adjoint_residual(self, ys, y_obss, fhats, xhats, gxs=None, gfs=None, losses=None):
+        if gxs is None:
+            gxs = [torch.empty((c,) + p.sx, device=self.device) for p, c in zip(self.plans, self.counts)]
+        if gfs is None:
+            gfs = [torch.empty((c, p.K) + p.sf, device=self.device) for p, c in zip(self.plans, self.counts)]
+        if losses is None:
+            losses = [torch.empty(c, dtype=torch.float64, device=self.device) for c in self.counts]
+        _lib.check(self.lib.eff_batch_adjoint_residual(
+            self._h, self._ptrs(ys), self._ptrs(y_obss), self._ptrs(fhats), self._ptrs(xhats),
+            self._ptrs(gxs), self._ptrs(gfs), self._ptrs(losses), _stream(self.device)))
+        return losses, gxs, gfs
+
+    def loss_grad(self, xs, fs, y_obss, losses=None, gxs=None, gfs=None):
+        """Loss and both gradients for every image: two persistent launches."""
+        if self._work is None:
+            self._work = ([torch.empty((c,) + p.sy, device=self.device) for p, c in zip(self.plans, self.counts)],
+                          [p.empty_spectrum(c) for p, c in zip(self.plans, self.counts)],
+                          [p.empty_spectrum(c) for p, c in zip(self.plans, self.counts)])
+        ys, xh, fh = self._work
+        self.forward_both(xs, fs, ys, xh, fh)
+        return self.adjoint_residual(ys, y_obss, fh, xh, gxs, gfs, losses)
+
+
+def set_cluster_mode(mode: int) -> None:
+    """0: per call (default); 1: one CTA per patch; 2: a 2-CTA cluster."""
+    _lib.check(_lib.load().eff_set_cluster_mode(int(mode)))
