@@ -56,7 +56,7 @@ def test_persistent_batch_matches_single_launches(cuda, specs, counts):
         l1, gx1, gf1 = plan.loss_grad(x, f, y_obs)
         assert rel(gxs[i].cpu(), gx1.cpu()) < TOL
         assert rel(gfs[i].cpu(), gf1.cpu()) < TOL
-        assert rel(losses[i].cpu(), l1.cpu()) < 1e-9
+        assert rel(losses[i].cpu(), l1.cpu()) < 1e-6
 
 
 def test_persistent_batch_matches_oracle(cuda):
