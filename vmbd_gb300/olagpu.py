@@ -97,3 +97,37 @@ class OlaGPU:
         else:
             _, out = self.plan.adjoint(t, xhat=self.fft_gpu, want_image=False, adjoint=self.adjoint)
         return out.cpu().numpy() if host else out
+
+    # -- optimisation support ---------------------------------------------
+    @property
+    def operand_shape(self):
+        """Shape of what ``cnv`` takes: the image (F) or the PSF stack (X)."""
+        if self.__id__ == "F":
+            return tuple(self.winaux.sx)
+        return (self.winaux.K,) + tuple(self.sf)
+
+    def objective(self, u: torch.Tensor, y: torch.Tensor):
+        """(0.5 ||Z u - y||^2 as a float, its gradient Z^T (Z u - y)): one
+        fused forward and one fused adjoint of the residual (the pair of
+        cnvinv_objfun / cnvinv_gradfun, olaGPU.py:756-811, without their
+        host round trips)."""
+        u = u.to(torch.float32).contiguous()
+        y = y.to(torch.float32).contiguous()
+        if self.__id__ == "F":
+            yp = self.plan.forward_image(u, self.fft_gpu)
+            loss, g, _ = self.plan.adjoint_residual(yp, y, fhat=self.fft_gpu, want_psf=False,
+                                                    adjoint=self.adjoint)
+        else:
+            yp = self.plan.forward_psf(u, self.fft_gpu)
+            loss, _, g = self.plan.adjoint_residual(yp, y, xhat=self.fft_gpu, want_image=False,
+                                                    adjoint=self.adjoint)
+        return float(loss), g
+
+    def deconv(self, y, z0=None, mode="lbfgsb", maxfun=100, alpha=0.0, beta=0.01, verbose=-1, m=5):
+        """OlaGPU.deconv (olaGPU.py:315-412) for mode 'lbfgsb': the PSFs (X
+        object) or the image (F object) minimising 0.5||y - Z u||^2 +
+        0.5 beta ||u||^2, u >= 0.  Returns (u, f(u), info)."""
+        if mode != "lbfgsb":
+            raise NotImplementedError("Not a valid mode!")
+        from .optim import deconv_lbfgsb
+        return deconv_lbfgsb(self, y, z0=z0, maxfun=maxfun, alpha=alpha, beta=beta, verbose=verbose, m=m)
