@@ -315,6 +315,25 @@ def profile_run(args, dev):
     """The step, eagerly, warmup + steps times (no graph, no comparators)."""
     import torch
     from vmbd_gb300.eff import EffPlan
+    if args.workload == "mfbd":
+        from vmbd_gb300.mfbd import OnlineMFBD, make_sequence
+        M = OnlineMFBD(MFBD["sy"], MFBD["sf"], MFBD["csf"], n_pg=MFBD["n_pg"], n_mu=MFBD["n_mu"], device=dev)
+        _, _, ys = make_sequence(M.plan, args.warmup + args.steps, seed=11)
+        M.init_latent(ys[:1])
+        for t in range(args.warmup + args.steps):
+            M.frame(ys[t])
+        torch.cuda.synchronize(dev)
+        print(json.dumps({"profile": "mfbd", "frames": args.warmup + args.steps}))
+        return
+    if args.workload == "cfg4":
+        from vmbd_gb300.eff import EffBatch
+        plans, counts, xs, fs, yo = cfg4_data(dev)
+        B = EffBatch(plans, counts)
+        for _ in range(args.warmup + args.steps):
+            B.loss_grad(xs, fs, yo)
+        torch.cuda.synchronize(dev)
+        print(json.dumps({"profile": "cfg4", "steps": args.warmup + args.steps}))
+        return
     w = WORKLOADS[args.workload]
     wa, x_np, f_np = make_inputs(w, seed=0)
     plan = EffPlan(wa, w["sf"], "valid", device=dev)
@@ -399,11 +418,10 @@ def run_mfbd(args, dev, n_timed, with_unfused=True):
     return out
 
 
-def run_cfg4(args, dev, n_timed):
-    """Images/s of the loss/gradient step over the uneven 64-image batch with
-    the autotuner's strategy (every candidate's time is reported)."""
+def cfg4_data(dev):
+    """Plans and seeded data of the uneven 64-image batch."""
     import torch
-    from vmbd_gb300 import autotune, geometry, synth
+    from vmbd_gb300 import geometry, synth
     from vmbd_gb300.eff import EffPlan
     plans, counts, xs, fs, yo = [], [], [], [], []
     for ci, (sx, csf, sf, kind, count) in enumerate(CFG4):
@@ -422,6 +440,14 @@ def run_cfg4(args, dev, n_timed):
         xs.append(x)
         fs.append(f)
         yo.append(y)
+    return plans, counts, xs, fs, yo
+
+
+def run_cfg4(args, dev, n_timed):
+    """Images/s of the loss/gradient step over the uneven 64-image batch with
+    the autotuner's strategy (every candidate's time is reported)."""
+    from vmbd_gb300 import autotune
+    plans, counts, xs, fs, yo = cfg4_data(dev)
     best, times = autotune.tune(plans, counts, xs, fs, yo)
     runner = autotune.BatchRunner(plans, counts, best)
     ms, _, _ = autotune.time_step(runner, xs, fs, yo, reps=max(3, n_timed), warmup=args.warmup)
@@ -486,7 +512,7 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=list(WORKLOADS) + ["mfbd"], default="cfg2")
+    ap.add_argument("--workload", choices=list(WORKLOADS) + ["mfbd", "cfg4"], default="cfg2")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile", action="store_true",
                     help="short eager run of the step only (for an ncu launch list / capture)")
@@ -496,8 +522,15 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
-    if args.workload == "mfbd":
+    if args.workload == "mfbd" and not args.profile:
         return main_mfbd(args, world, rank, local)
+    if args.workload == "cfg4" and not args.profile:
+        return main_cfg4(args, world, rank, local)
+    if args.profile:
+        import torch
+        torch.cuda.set_device(local)
+        profile_run(args, torch.device("cuda", local))
+        return
     w = WORKLOADS[args.workload]
     pixels = w["sx"][0] * w["sx"][1]
     metric = "EFF fwd+adjoint Mpixel/s"
@@ -604,6 +637,34 @@ def main():
                                          "note": "adjoints of the same residual y_gpu - y_obs"}
     if rank == 0:
         print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main_cfg4(args, world, rank, local):
+    """``--workload cfg4``: images/s of the uneven 64-image batch."""
+    import torch
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps({"impl": "reference", "metric": "uneven batch images/s",
+                              "unavailable": "the reference has no batched path; see --workload cfg2"}))
+        return
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    R = run_cfg4(args, dev, n_timed=args.steps)
+    ms = allreduce_max(R["ms_per_step"], world, dev)
+    if rank == 0:
+        print(json.dumps({
+            "metric": "uneven batch images/s", "value": world * 64 / (ms * 1e-3), "unit": "images/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": {"workload": "cfg4", "desc": R["config"],
+                                            "strategy": R["strategy"], "candidates_ms": R["candidates_ms"]},
+        }))
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
