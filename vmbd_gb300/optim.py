@@ -146,9 +146,9 @@ class PBB:
 def deconv_lbfgsb(Z, y, z0=None, maxfun=100, alpha=0.0, beta=0.01, verbose=-1, m=5):
     """OlaGPU.deconv(y, mode='lbfgsb'), olaGPU.py:381-412: minimise
     0.5||y - Z u||^2 + 0.5 beta ||u||^2 over u >= 0 with scipy's L-BFGS-B
-    (factr 10, pgtol 1e-14, bounds [0, inf)).  ``z0`` defaults to Z^T y.
-    Returns (u, f(u), info) like fmin_l_bfgs_b."""
-    from scipy.optimize import fmin_l_bfgs_b
+    (the reference's factr 10 and pgtol 1e-14, bounds [0, inf)).  ``z0``
+    defaults to Z^T y.  Returns (u, f(u), info) like fmin_l_bfgs_b."""
+    from scipy.optimize import minimize
     if alpha > 0:
         raise NotImplementedError("the gradient (Laplacian) regulariser is not on this path")
     dev = Z.device
@@ -170,6 +170,9 @@ def deconv_lbfgsb(Z, y, z0=None, maxfun=100, alpha=0.0, beta=0.01, verbose=-1, m
         g = grad.double().cpu().numpy().ravel() + beta * z
         return obj, g
 
-    res = fmin_l_bfgs_b(fg, z0, factr=10.0, pgtol=10e-15, maxfun=maxfun, bounds=[(0.0, None)] * z0.size,
-                        m=m, iprint=verbose)
-    return np.reshape(res[0], shape), res[1], res[2]
+    r = minimize(fg, z0, jac=True, method="L-BFGS-B", bounds=[(0.0, None)] * z0.size,
+                 options={"maxfun": maxfun, "maxcor": m, "ftol": 10.0 * np.finfo(float).eps, "gtol": 10e-15,
+                          "disp": verbose > 0})
+    info = {"grad": r.jac, "funcalls": r.nfev, "nit": r.nit, "warnflag": 0 if r.success else 1,
+            "task": r.message}
+    return np.reshape(r.x, shape), float(r.fun), info
