@@ -171,8 +171,9 @@ def deconv_lbfgsb(Z, y, z0=None, maxfun=100, alpha=0.0, beta=0.01, verbose=-1, m
         return obj, g
 
     r = minimize(fg, z0, jac=True, method="L-BFGS-B", bounds=[(0.0, None)] * z0.size,
-                 options={"maxfun": maxfun, "maxcor": m, "ftol": 10.0 * np.finfo(float).eps, "gtol": 10e-15,
-                          "disp": verbose > 0})
+                 options={"maxfun": maxfun, "maxcor": m, "ftol": 10.0 * np.finfo(float).eps, "gtol": 10e-15})
+    if verbose > 0:
+        print(f"L-BFGS-B: {r.nfev} evaluations, f = {r.fun:.6g}: {r.message}")
     info = {"grad": r.jac, "funcalls": r.nfev, "nit": r.nit, "warnflag": 0 if r.success else 1,
             "task": r.message}
     return np.reshape(r.x, shape), float(r.fun), info
