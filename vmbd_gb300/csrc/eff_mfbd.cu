@@ -37,10 +37,24 @@ __global__ void __launch_bounds__(kMfbdThreads) dots3_kernel(const float* a, con
   s0 = warp_sum(s0);
   s1 = warp_sum(s1);
   s2 = warp_sum(s2);
-  if ((threadIdx.x & 31) == 0) {
-    atomicAdd(out, s0);
-    atomicAdd(out + 1, s1);
-    atomicAdd(out + 2, s2);
+  // one atomic per block and value (per-warp atomics on the same three
+  // addresses serialise)
+  __shared__ double part[3][kMfbdThreads / 32];
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) {
+    part[0][w] = s0;
+    part[1][w] = s1;
+    part[2][w] = s2;
+  }
+  __syncthreads();
+  if (w == 0) {
+    const int nw = blockDim.x >> 5;
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      double v = l < nw ? part[q][l] : 0.0;
+      v = warp_sum(v);
+      if (l == 0) atomicAdd(out + q, v);
+    }
   }
 }
 
@@ -122,6 +136,23 @@ __global__ void __launch_bounds__(kMfbdThreads) pg_step_kernel(float* f, const f
   for (int i = threadIdx.x; i < n; i += blockDim.x) f[base + i] = fmaxf(v[i] - tau, 0.f);
 }
 
+// Block maximum of a non-negative value, then one atomicMax on its bits
+// (non-negative floats order like their bit patterns).
+__device__ __forceinline__ void block_max_atomic(float m, unsigned* bits) {
+  __shared__ float part[kMfbdThreads / 32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) part[w] = m;
+  __syncthreads();
+  if (w == 0) {
+    float v = l < (int)(blockDim.x >> 5) ? part[l] : 0.f;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if (l == 0) atomicMax(bits, __float_as_uint(fmaxf(v, 0.f)));
+  }
+}
+
 // out_bits <- max(0, max_i a[i]) as float bits (non-negative floats order
 // like their bit patterns).
 __global__ void __launch_bounds__(kMfbdThreads) max_nonneg_kernel(const float* a, long long n, unsigned* out_bits) {
@@ -129,9 +160,7 @@ __global__ void __launch_bounds__(kMfbdThreads) max_nonneg_kernel(const float* a
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
        t += (long long)gridDim.x * blockDim.x)
     m = fmaxf(m, a[t]);
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-  if ((threadIdx.x & 31) == 0) atomicMax(out_bits, __float_as_uint(m));
+  block_max_atomic(m, out_bits);
 }
 
 // x *= max(num / (den + tol), tol); xmax_bits <- max over the interior
@@ -156,9 +185,7 @@ __global__ void __launch_bounds__(kMfbdThreads) mu_update_kernel(float* x, const
     const int i = int(t / cols), j = int(t % cols);
     if (i >= b0 && i < rows - b0 && j >= b1 && j < cols - b1) m = fmaxf(m, xv);
   }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-  if ((threadIdx.x & 31) == 0) atomicMax(xmax_bits, __float_as_uint(fmaxf(m, 0.f)));
+  block_max_atomic(m, xmax_bits);
 }
 
 __global__ void __launch_bounds__(kMfbdThreads) clamp_max_kernel(float* x, long long n, const unsigned* xmax_bits) {
@@ -168,9 +195,11 @@ __global__ void __launch_bounds__(kMfbdThreads) clamp_max_kernel(float* x, long 
     x[t] = fminf(x[t], mx);
 }
 
+// Grid for n elements: at most 4 elements per thread before growing the
+// grid, capped at 2 blocks per SM of a 152-SM part.
 static int grid_for(long long n) {
-  const long long b = (n + kMfbdThreads - 1) / kMfbdThreads;
-  return (int)(b < 1216 ? (b < 1 ? 1 : b) : 1216);
+  const long long b = (n + 4LL * kMfbdThreads - 1) / (4LL * kMfbdThreads);
+  return (int)(b < 304 ? (b < 1 ? 1 : b) : 304);
 }
 
 cudaError_t launch_dots3(const float* a, const float* ap, long long na, const float* b, const float* bp,
