@@ -268,7 +268,17 @@ int eff_plan_create(const EffGeom* geom, const float* win0, const float* win1, E
       if (worst <= kSmemLimit || p.threads <= 128) break;
       p.threads /= 2;
     }
-    p.threads2 = p.N >= 128 ? 256 : 128;
+    // 2-CTA clusters: the same rule on each CTA's half of the frame.
+    p.threads2 = eff::max_threads(p.N);
+    for (;;) {
+      size_t worst = 0;
+      for (int op = 0; op < eff::kNumOps; ++op) {
+        const size_t s = eff::smem_bytes(p.N, op, P, p.threads2, 2);
+        if (s > worst) worst = s;
+      }
+      if (worst <= kSmemLimit || p.threads2 <= 128) break;
+      p.threads2 /= 2;
+    }
   }
 
   cudaError_t e = cudaGetDevice(&p.device);
