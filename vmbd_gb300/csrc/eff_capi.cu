@@ -5,6 +5,7 @@
 // twiddle table, and picks the FFT frame.  The compute entry points only
 // enqueue work on the caller's stream (memset of atomically accumulated
 // outputs + one kernel) and allocate nothing.
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstdio>
@@ -268,8 +269,10 @@ int eff_plan_create(const EffGeom* geom, const float* win0, const float* win1, E
       if (worst <= kSmemLimit || p.threads <= 128) break;
       p.threads /= 2;
     }
-    // 2-CTA clusters: the same rule on each CTA's half of the frame.
-    p.threads2 = eff::max_threads(p.N);
+    // 2-CTA clusters: one lane group per column unit a CTA owns (N/4 units
+    // of N/16 lanes), at most the compiled maximum, halved while the frame
+    // half plus the exchange scratch does not fit.
+    p.threads2 = std::min(eff::max_threads(p.N), std::max(128, p.N * p.N / 64));
     for (;;) {
       size_t worst = 0;
       for (int op = 0; op < eff::kNumOps; ++op) {
