@@ -65,7 +65,15 @@ struct Params {
   const float2* win1;      // window factors (alpha, gamma) [csf1, sw1]
   const float2* tw;        // W_N table [16*G]
   long long x_bs, f_bs, y_bs, spec_bs, out0_bs, out1_bs;  // per-image strides
+  const char* pf;          // forward: bytes [pf, pf + pf_bytes) to bring into L2 for the next kernel
+  long long pf_bytes;
 };
+
+// TMA bulk prefetch of a contiguous range into L2 (16-byte aligned start and
+// size, sm_90+).
+__device__ __forceinline__ void l2_prefetch_bulk(const void* p, unsigned bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
 
 // Half-spectrum bins a CTA stores per row: all N/2+1 (CL = 1) or its
 // quarter plus, on CTA 0, the N/2 bin (CL = 2).
@@ -439,22 +447,17 @@ __device__ __forceinline__ void eff_patch(const Params& P, int k, long long b, f
 
   for (int i = tid; i < N; i += blockDim.x) tw[i] = __ldg(P.tw + i);
 
-  // Loss of the residual: this CTA's contiguous share of the pixels.
-  if constexpr (OP == OP_ADJ) {
-    if (P.loss && T.y_obs) {
-      const long long npx = (long long)P.sy0 * P.sy1;
-      const long long chunk = (npx + ncta - 1) / ncta;
-      const long long p0 = (long long)cta * chunk;
-      const long long p1 = min(npx, p0 + chunk);
-      float acc = 0.f;
-      for (long long p = p0 + tid; p < p1; p += blockDim.x) {
-        const float r = __ldg(T.y + p) - __ldg(T.y_obs + p);
-        acc = fmaf(r, r, acc);
-      }
-      double d = acc;
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
-      if ((tid & 31) == 0) atomicAdd(P.loss + b, 0.5 * d);
+  // Fused forward of a loss/gradient step: start pulling the observation
+  // the adjoint will read into L2 (this CTA's 16-byte-aligned share).
+  if constexpr (OP == OP_FWD_BOTH) {
+    if (P.pf && tid == 0) {
+      const long long per = ((P.pf_bytes + ncta - 1) / ncta + 15) & ~15LL;
+      const long long o0 = (long long)cta * per;
+      long long n = min(per, P.pf_bytes - o0);
+      n &= ~15LL;
+      const char* a = P.pf + b * P.pf_bytes + o0;
+      if (n > 0 && (reinterpret_cast<unsigned long long>(a) & 15ull) == 0)
+        l2_prefetch_bulk(a, (unsigned)n);
     }
   }
   // The peer must not write into this CTA's frame before it is running (and,
@@ -594,6 +597,25 @@ __device__ __forceinline__ void eff_patch(const Params& P, int k, long long b, f
           }
         }
       }
+    }
+  }
+  // Loss of the residual: this CTA's contiguous share of the pixels (after
+  // the transforms, when the observation is in L2).
+  if constexpr (OP == OP_ADJ) {
+    if (P.loss && T.y_obs) {
+      const long long npx = (long long)P.sy0 * P.sy1;
+      const long long chunk = (npx + ncta - 1) / ncta;
+      const long long p0 = (long long)cta * chunk;
+      const long long p1 = min(npx, p0 + chunk);
+      float acc = 0.f;
+      for (long long p = p0 + tid; p < p1; p += blockDim.x) {
+        const float r = __ldg(T.y + p) - __ldg(T.y_obs + p);
+        acc = fmaf(r, r, acc);
+      }
+      double d = acc;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+      if ((tid & 31) == 0) atomicAdd(P.loss + b, 0.5 * d);
     }
   }
   // Peers read this CTA's frame in phase 3: stay resident until they finish.
