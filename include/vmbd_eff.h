@@ -54,8 +54,10 @@ typedef struct EffGeom {
   int csf[2];  /* patch grid */
   int sw[2];   /* patch size */
   int hop[2];  /* patch hop */
-  int sfft;    /* FFT frame edge: 0 = smallest power of two >= max(E) (>= 64) */
+  int sfft;    /* FFT frame edge, 64, 128, 192 or 256 (>= max(E)); 0 = the smallest power of two >= max(E) */
   int mode;    /* EFF_MODE_* */
+  int threads; /* CTA size, a multiple of 32 up to 512 (384 for the 192 frame); 0 = the
+                  largest that fits.  Lowered to fit shared memory. */
 } EffGeom;
 
 typedef struct EffPlan EffPlan;
@@ -157,6 +159,23 @@ int eff_basis_project(const float* fs, const float* basis, float* w, int nb, int
  * the product of the two windows' maxima, sf made odd). */
 int eff_edgetaper(float* im, int rows, int cols, const float* wy, int hy, const float* wx, int hx,
                   int batch, void* stream);
+
+/* Fourier-division deconvolution, OlaGPU.deconv(y, mode='xdirect'),
+ * olaGPU.py:550-609 with comp_ola_deconv_Kernel gputools.cu:316-341.  Per
+ * patch k: the chop of y [batch, sy0, sy1] placed at frame offset off
+ * (sf-1 valid, floor(sf/2) same) times the window at the frame origin, its
+ * FFT Y, Z = conj(S) Y / (|S|^2 + alpha L + beta) with
+ * L = |FFT([-1 1])|^2 + |FFT([-1; 1])|^2 over the plan's N x N frame, the
+ * inverse FFT z; then
+ *   u  [batch, sx0, sx1] (S = fhat, F object): overlap-add of the sw x sw
+ *      crops of z (no window), cropped to sx;
+ *   fz [batch, K, sf0, sf1] (S = xhat, X object): the sf x sf crops of z.
+ * Either output may be NULL (not both); both are overwritten.  The division
+ * happens in the plan's frame, so results equal the reference's when the
+ * plan's N is the reference's frame (the power of two >= sw + sf - 1 in
+ * both dims).  EFF_ERR_UNSUPPORTED for mode full (olaGPU.py:570-571). */
+int eff_deconv_xdirect(const EffPlan* plan, const float* y, const void* fhat, const void* xhat, float* u,
+                       float* fz, float alpha, float beta, int batch, void* stream);
 
 /* eff_adjoint of mask .* y (mask [batch, sy0, sy1]) without forming the
  * product: Ft(m y) of the multiplicative image step, vmbd_chimney.py:143. */

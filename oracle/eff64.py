@@ -486,3 +486,141 @@ def edgetaper(x, sf) -> np.ndarray:
         elif j > C - 1 - hsf[1]:
             cx[j] = wx[C - 1 - j]
     return x * ry[:, None] * cx[None, :]
+
+
+# --------------------------------------------------------------------------
+# Fourier-division deconvolution (OlaGPU.deconv 'xdirect' / 'direct')
+# --------------------------------------------------------------------------
+
+
+def psf_spectrum(f, g: Geometry) -> np.ndarray:
+    """F-hat of an F object: FFT of the zero-padded PSFs (olaGPU.py:142-157),
+    half spectrum (``rfft2``) of the ``sfft`` frame."""
+    return _rfft2(pad_stack(np.asarray(f, np.float64), g.sfft))
+
+
+def image_spectrum(x, g: Geometry, ws) -> np.ndarray:
+    """X-hat of an X object: FFT of the windowed, zero-padded patches
+    (olaGPU.py:147-157), half spectrum."""
+    return _rfft2(windowed_patches(x, g, ws, g.sfft))
+
+
+def laplacian_spectrum(sz) -> np.ndarray:
+    """``L = |FFT(gx)|^2 + |FFT(gy)|^2`` of the difference filters
+    ``gx = [[-1, 1]]`` and ``gy = [[-1], [1]]`` zero-padded to the frame
+    (olaGPU.py:553-561): ``|e^{-2 pi i k/n} - 1|^2 = 4 sin^2(pi k/n)``, full
+    ``sz`` frame."""
+    k0 = np.arange(int(sz[0]))
+    k1 = np.arange(int(sz[1]))
+    return (4.0 * np.sin(np.pi * k0 / sz[0]) ** 2)[:, None] + (4.0 * np.sin(np.pi * k1 / sz[1]) ** 2)[None, :]
+
+
+def deconv_xdirect(y, Sh, g: Geometry, ws, target: str, alpha: float = 0.0, beta: float = 0.01) -> np.ndarray:
+    """OlaGPU.deconv(y, mode='xdirect'), olaGPU.py:550-609: per-patch
+    regularised division in Fourier space.
+
+    * patches of ``y``: ``chop_pad(y, offset)`` with ``offset = sf - 1``
+      (valid) or ``floor(sf/2)`` (same), times the window stack placed at
+      the frame origin (``pad_stack(ws)``), olaGPU.py:573-584 -- the two
+      supports overlap on ``[offset, sw)``;
+    * ``Z = conj(S) Y / (|S|^2 + alpha L + beta)`` with ``S`` the cached
+      spectrum (F-hat of an F object, X-hat of an X object):
+      comp_ola_deconv_Kernel gputools.cu:316-341; ``L`` as
+      ``laplacian_spectrum`` when ``alpha > 0``, else 0;
+    * inverse FFT (olaGPU.py:593-595), then ``target='psf'`` (X object):
+      crop each slice to ``sf`` (:598-600); ``target='image'`` (F object):
+      crop to ``sw``, overlap-add with extent ``sw`` (no window), crop to
+      ``sx`` (:602-607).
+
+    ``Sh`` is the half spectrum ``[K, N0, N1//2+1]`` (``psf_spectrum`` /
+    ``image_spectrum``).  The edgetaper of ``y`` at olaGPU.py:566-567 acts
+    on a copy that the chop does not read (it chops the argument ``y``), so it
+    does not change the result and is not restated.
+    """
+    if g.mode == "valid":
+        off = tuple(v - 1 for v in g.sf)
+    elif g.mode == "same":
+        off = tuple(v // 2 for v in g.sf)
+    else:
+        raise NotImplementedError("Not a valid mode!")
+    N = g.sfft
+    yp = chop_pad(np.asarray(y, np.float64), g.csf, g.sw, g.hop, N, off) * pad_stack(np.asarray(ws, np.float64), N)
+    Yh = _rfft2(yp)
+    den = np.abs(Sh) ** 2 + beta
+    if alpha > 0:
+        den = den + alpha * laplacian_spectrum(N)[:, : N[1] // 2 + 1]
+    z = _irfft2(np.conj(Sh) * Yh / den, s=N)
+    if target == "psf":
+        return crop_stack(z, g.sf)
+    if target != "image":
+        raise ValueError("target must be 'image' or 'psf'")
+    return crop(ola(crop_stack(z, g.sw), g.csf, g.sw, g.hop), g.sx)
+
+
+def impad(y, sz) -> np.ndarray:
+    """Replicate padding by ``sz`` with ``floor(sz/2)`` rows/columns before:
+    impad kernel.cu:244-266 via impad_gpu gputools.py:884-907."""
+    sz = np.asarray(sz, dtype=np.int64)
+    top, left = int(sz[0] // 2), int(sz[1] // 2)
+    return np.pad(np.asarray(y, np.float64), ((top, int(sz[0]) - top), (left, int(sz[1]) - left)), mode="edge")
+
+
+def deconv_direct(y, Fh, g: Geometry, ws, alpha: float = 0.0, beta: float = 0.01, edgetapering: int = 1,
+                  factor: int = 3) -> np.ndarray:
+    """OlaGPU.deconv(y, mode='direct') of an F object, olaGPU.py:515-548:
+    ``xdirect`` of ``y`` clipped at 0, divided by the ``xdirect`` of a
+    constant image (edgetapered by ``2 sf`` before and after, clipped to
+    [0.01, 10]) to undo the window's ripple; the border
+    ``factor * sf + 1`` wide is cropped (offset ``floor((factor*sf - 1)/2)``)
+    and refilled by replicate padding."""
+    sf = np.asarray(g.sf, dtype=np.int64)
+    u = cliplower(deconv_xdirect(y, Fh, g, ws, "image", alpha, beta), 0.0)
+    const = np.ones(g.sy)
+    if edgetapering == 1:
+        const = edgetaper(const, 2 * sf)
+    c = deconv_xdirect(const, Fh, g, ws, "image", alpha, beta)
+    c = clipupper(cliplower(edgetaper(c, 2 * sf), 0.01), 10.0)
+    u = u / c
+    sz = np.asarray(u.shape, dtype=np.int64)
+    csz = sz - factor * sf - 1
+    off = np.floor((factor * sf - 1) / 2.0).astype(np.int64)
+    u = crop(u, csz, off)
+    return impad(u, sz - csz)
+
+
+def deconv_xdirect_fp32(y, operand, g: Geometry, ws, target: str, alpha: float = 0.0,
+                        beta: float = 0.01) -> np.ndarray:
+    """``deconv_xdirect`` in the reference's own precision: every array
+    complex64/float32 and the FFTs single precision (``scipy.fft`` on float32
+    input), as pyfft computes them (olaGPU.py:155, 586-595).  ``operand`` is
+    the PSF stack (``target='image'``, F object) or the image
+    (``target='psf'``, X object).
+
+    Used to state how far an FP32 pipeline can be from the FP64 result: the
+    PSF estimate divides by ``|X-hat|^2``, whose dynamic range (~1e9 for a
+    windowed image patch) turns FFT rounding into a relative error of a few
+    1e-5, for any FP32 implementation."""
+    if g.mode == "valid":
+        off = tuple(v - 1 for v in g.sf)
+    elif g.mode == "same":
+        off = tuple(v // 2 for v in g.sf)
+    else:
+        raise NotImplementedError("Not a valid mode!")
+    N = g.sfft
+    f32 = np.float32
+    wsp = pad_stack(np.asarray(ws, np.float64), N).astype(f32)
+    yp = chop_pad(np.asarray(y, np.float64), g.csf, g.sw, g.hop, N, off).astype(f32) * wsp
+    Yh = scipy.fft.rfft2(yp)
+    if target == "image":
+        Sh = scipy.fft.rfft2(pad_stack(np.asarray(operand, np.float64), N).astype(f32))
+    elif target == "psf":
+        Sh = scipy.fft.rfft2(chop_pad(np.asarray(operand, np.float64), g.csf, g.sw, g.hop, N).astype(f32) * wsp)
+    else:
+        raise ValueError("target must be 'image' or 'psf'")
+    den = (Sh.real * Sh.real + Sh.imag * Sh.imag).astype(f32) + f32(beta)
+    if alpha > 0:
+        den = den + f32(alpha) * laplacian_spectrum(N)[:, : N[1] // 2 + 1].astype(f32)
+    z = scipy.fft.irfft2((np.conj(Sh) * Yh / den).astype(np.complex64), s=N)
+    if target == "psf":
+        return crop_stack(z, g.sf)
+    return crop(ola(crop_stack(z, g.sw), g.csf, g.sw, g.hop), g.sx)

@@ -6,11 +6,12 @@ never on a GPU machine and never by the product.
 
 What runs is the reference itself, not a restatement:
 
-* the Python source of ``OlaGPU.__init__/cnv/cnvtp/fft`` (olaGPU.py:95-311,
-  813-824), ``window`` and ``win2winaux`` (imagetools.py:314-344, 398-454)
-  and the ``gputools`` wrappers on the path (gputools.py:322-401, 546-569,
-  599-640, 1025-1044, 1068-1181), read from the reference files and
-  executed unchanged except for the one substitution below;
+* the Python source of ``OlaGPU.__init__/cnv/cnvtp/fft/deconv``
+  (olaGPU.py:95-311, 312-733, 813-824; ``deconv`` is run in its 'xdirect'
+  mode), ``window`` and ``win2winaux`` (imagetools.py:314-344, 398-454) and
+  the ``gputools`` wrappers on the path (gputools.py:322-401, 498-519,
+  546-569, 599-640, 1025-1044, 1068-1181), read from the reference files
+  and executed unchanged except for the substitutions below;
 * the reference's CUDA kernels (gputools.cu) compiled for the CPU into
   ``oracle/_ref`` by ``oracle/build_ref.py``, launched with the grid and
   block sizes the wrappers compute.
@@ -173,6 +174,8 @@ class _Plan:
         self.shape = tuple(int(v) for v in shape)
 
     def execute(self, ptr, batch=1):
+        if isinstance(ptr, np.ndarray):  # pyfft also takes the array itself
+            ptr = ptr.gpudata
         n = batch * self.shape[0] * self.shape[1]
         buf = (ctypes.c_float * (2 * n)).from_address(int(ptr))
         a = np.frombuffer(buf, dtype=np.complex64).reshape((batch,) + self.shape)
@@ -253,7 +256,7 @@ def load():
                                     "cubin": None})
     for fn in ("chop_mod_pad_GPU", "chop_pad_GPU", "crop_gpu2cpu", "crop_stack_GPU",
                "normalize", "ola_GPU_test", "pad_cpu2gpu", "pad_stack_GPU",
-               "cliplower_GPU", "clipupper_GPU"):
+               "cliplower_GPU", "clipupper_GPU", "comp_ola_deconv"):
         exec(compile(_era_compat(_top_level_block(gt_lines, fn)), f"gputools.py:{fn}", "exec"),
              gputools.__dict__)
 
@@ -265,11 +268,11 @@ def load():
              imagetools.__dict__)
 
     ola_lines = _source_lines("olaGPU.py")
-    methods = {m: _method_block(ola_lines, m) for m in ("__init__", "cnv", "cnvtp", "fft")}
+    methods = {m: _method_block(ola_lines, m) for m in ("__init__", "cnv", "cnvtp", "fft", "deconv")}
     bad = "self.winaux.sw+self.sf-1,"
     assert methods["cnvtp"].count(bad) == 1, "cnvtp overlap-add extent not found"
     methods["cnvtp"] = methods["cnvtp"].replace(bad, "self.winaux.sw,")
-    src = "class OlaGPU:\n" + "\n".join(methods[m] for m in ("__init__", "cnv", "cnvtp", "fft"))
+    src = "class OlaGPU:\n" + "\n".join(methods[m] for m in ("__init__", "cnv", "cnvtp", "fft", "deconv"))
     olaGPU = _module("olaGPU", {"np": np, "cua": cua, "cufft": cufft, "gputools": gputools})
     exec(compile(_era_compat(src), "olaGPU.py:OlaGPU", "exec"), olaGPU.__dict__)
     return gputools, imagetools, olaGPU

@@ -58,6 +58,10 @@ void ref_zeroPadKernel(G, float* dx, int m, int n, float* dy, int p, int q, int 
   RUN(zeroPadKernel(dx, m, n, dy, p, q, s, t));
 }
 
+void ref_zeroPadComplexKernel(G, cufftComplex* dx, int m, int n, float* dy, int p, int q, int s, int t) {
+  RUN(zeroPadComplexKernel(dx, m, n, dy, p, q, s, t));
+}
+
 void ref_chop_pad_Kernel(G, float* dx, int xm, int xn, int xr, float* dy, int ym, int yn, int wm,
                          int wn, int om, int on, int cm, int cn, int hopm, int hopn) {
   RUN(chop_pad_Kernel(dx, xm, xn, xr, dy, ym, yn, wm, wn, om, on, cm, cn, hopm, hopn));
@@ -101,6 +105,11 @@ void ref_ola_ComplexKernel_test(G, float* out, cufftComplex* in, unsigned outm, 
                                 unsigned on, unsigned cm, unsigned cn, unsigned hopm,
                                 unsigned hopn) {
   RUN(ola_ComplexKernel_test(out, in, outm, outn, inm, inn, wm, wn, om, on, cm, cn, hopm, hopn));
+}
+
+void ref_comp_ola_deconv_Kernel(G, cufftComplex* out, int outk, int outm, int outn, cufftComplex* f,
+                                cufftComplex* y, cufftComplex* L, float alpha, float beta) {
+  RUN(comp_ola_deconv_Kernel(out, outk, outm, outn, f, y, L, alpha, beta));
 }
 
 }  // extern "C"

@@ -1,7 +1,7 @@
 """Generate the golden EFF fixtures in this directory from the reference.
 
-Runs the reference's own ``win2winaux``, ``OlaGPU.__init__/cnv/cnvtp`` and
-``gputools`` wrappers over its ``gputools.cu`` kernels compiled for the CPU
+Runs the reference's own ``win2winaux``, ``OlaGPU.__init__/cnv/cnvtp/deconv``
+and ``gputools`` wrappers over its ``gputools.cu`` kernels compiled for the CPU
 (``oracle/ref_harness.py``; pyfft replaced by a complex64 numpy FFT), in FP32
 as the reference computes, on small seeded cases, and stores inputs and
 outputs as ``ref_<case>.npz``.
@@ -74,10 +74,49 @@ def make_case(name, sx, csf, sf, mode, wa_sx, kind, seed, gputools, imagetools, 
           f"sfft={F.sfft_gpu} mode={mode} -> {os.path.basename(path)}")
 
 
+# Fourier-division deconvolution, OlaGPU.deconv(mode='xdirect') of an F object
+# (image estimate) and of an X object (PSF estimate):
+# name: (sx, csf, sf, mode, psf kind, seed, alpha, beta)
+DECONV_CASES = {
+    "deconv_valid": ((96, 96), (2, 2), (9, 9), "valid", "gauss", 21, 0.0, 0.01),
+    "deconv_same_laplacian": ((80, 112), (2, 3), (7, 7), "same", "motion", 22, 0.05, 1e-3),
+    "deconv_grid4x4": ((96, 96), (4, 4), (15, 15), "valid", "gauss", 23, 0.01, 0.01),
+}
+
+
+def make_deconv_case(name, sx, csf, sf, mode, kind, seed, alpha, beta, imagetools, olaGPU):
+    sx = np.array(sx)
+    sf = np.array(sf)
+    K = int(np.prod(csf))
+    wa = imagetools.win2winaux(sx, csf, 0.5)
+    x = synth.blob_edge_image(tuple(sx), seed=seed)
+    gen = synth.gaussian_psfs if kind == "gauss" else synth.motion_psfs
+    f = gen(K, tuple(sf), seed=seed + 100)
+    F = olaGPU.OlaGPU(f, sx, mode, wa)
+    y = np.asarray(F.cnv(x), np.float32)
+    y = (y + 0.01 * np.random.default_rng(seed + 200).standard_normal(y.shape)).astype(np.float32)
+    X = olaGPU.OlaGPU(rh.cua.to_gpu(x), sf, mode, wa)
+    # edgetapering=0: the taper in 'xdirect' acts on a copy the chop never
+    # reads (olaGPU.py:566-575), so the result is the same without it
+    u = np.asarray(F.deconv(y, mode="xdirect", alpha=alpha, beta=beta, edgetapering=0), np.float32)
+    fz = np.asarray(X.deconv(y, mode="xdirect", alpha=alpha, beta=beta, edgetapering=0), np.float32)
+    assert np.isfinite(u).all() and np.isfinite(fz).all()
+    out = dict(sx=sx, sf=sf, csf=np.array(csf), sw=np.array(wa.sw, dtype=int),
+               hop=np.array(wa.nhop, dtype=int), mode=np.array(mode), sfft=np.array(F.sfft_gpu),
+               alpha=np.array(alpha), beta=np.array(beta), x=x, f=f, y=y,
+               ws=np.asarray(wa.ws_gpu, np.float32), u=u, fz=fz)
+    path = os.path.join(HERE, f"ref_{name}.npz")
+    np.savez_compressed(path, **out)
+    print(f"{name}: sx={tuple(sx)} csf={csf} sf={tuple(sf)} sw={tuple(wa.sw)} sfft={F.sfft_gpu} "
+          f"mode={mode} alpha={alpha} beta={beta} -> {os.path.basename(path)}")
+
+
 def main():
     gputools, imagetools, olaGPU = rh.load()
     for name, spec in CASES.items():
         make_case(name, *spec, gputools, imagetools, olaGPU)
+    for name, spec in DECONV_CASES.items():
+        make_deconv_case(name, *spec, imagetools, olaGPU)
 
 
 if __name__ == "__main__":

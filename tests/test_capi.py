@@ -55,8 +55,14 @@ def test_plan_rejects_bad_geometry_without_gpu():
     g.mode = 7
     assert L.eff_plan_create(ctypes.byref(g), w, w, ctypes.byref(h)) == _lib.EFF_ERR_INVALID
     g.mode = 0
-    g.sfft = 96  # not a supported power of two
+    g.sfft = 96  # not a supported frame edge
     assert L.eff_plan_create(ctypes.byref(g), w, w, ctypes.byref(h)) == _lib.EFF_ERR_UNSUPPORTED
+    g.sfft = 0
+    for bad in (100, 1024, -32):  # CTA size: a multiple of 32 up to the compiled maximum
+        g.threads = bad
+        assert L.eff_plan_create(ctypes.byref(g), w, w, ctypes.byref(h)) == _lib.EFF_ERR_INVALID
+        assert b"threads" in L.eff_last_error()
+    g.threads = 0
     assert L.eff_plan_create(None, w, w, ctypes.byref(h)) == _lib.EFF_ERR_INVALID
 
 

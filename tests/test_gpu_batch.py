@@ -78,10 +78,35 @@ def test_autotuner_picks_a_strategy(cuda):
     plans = [c[0] for c in cls]
     args = ([c[1] for c in cls], [c[2] for c in cls], [c[3] for c in cls])
     best, times = autotune.tune(plans, (2, 2, 2), *args)
-    assert best in ("persistent", "per_class/cta", "per_class/cluster")
+    cands = autotune.candidates(plans)
+    assert best in cands and autotune.parse(best)[0] in autotune.STRATEGIES
     assert all(times[s] > 0 for s in ("persistent", "per_class/cta", "per_class/cluster"))
     ms, _, (losses, gxs, gfs) = autotune.time_step(autotune.BatchRunner(plans, (2, 2, 2), best), *args)
     for i, (plan, x, f, y_obs) in enumerate(cls):
         _, gx1, gf1 = plan.loss_grad(x, f, y_obs)
         assert rel(gxs[i].cpu(), gx1.cpu()) < TOL
         assert rel(gfs[i].cpu(), gf1.cpu()) < TOL
+
+
+@pytest.mark.parametrize("cand", ["per_class/cta@f192", "per_class/cluster@f192/t256", "persistent@f192"])
+def test_frame192_candidates_match_default_frames(cuda, cand):
+    """The autotuner's 192-frame candidates give the default frames' results
+    (the 384x512 class has extent 139, so it moves from 256 to 192).  The
+    observation is half the model image, so the residual is of the model's
+    size: a noise-sized residual would amplify the two frames' different
+    forward rounding ~100x into the gradients."""
+    from vmbd_gb300 import autotune
+    cls = [make_class(s, c, cuda, 5 * i) for i, (s, c) in enumerate(zip(WORKLOAD, (1, 2, 1)))]
+    cls = [(p, x, f, 0.5 * p.forward_both(x, f)) for p, x, f, _ in cls]
+    plans = [c[0] for c in cls]
+    assert cand in autotune.candidates(plans)
+    runner = autotune.BatchRunner(plans, (1, 2, 1), cand)
+    assert sorted(p.N for p in runner.plans) != sorted(p.N for p in plans)
+    assert 192 in [p.N for p in runner.plans]
+    args = ([c[1] for c in cls], [c[2] for c in cls], [c[3] for c in cls])
+    _, _, (losses, gxs, gfs) = autotune.time_step(runner, *args, reps=1, warmup=0)
+    for i, (plan, x, f, y_obs) in enumerate(cls):
+        l1, gx1, gf1 = plan.loss_grad(x, f, y_obs)
+        assert rel(gxs[i].cpu(), gx1.cpu()) < TOL
+        assert rel(gfs[i].cpu(), gf1.cpu()) < TOL
+        assert rel(losses[i].cpu(), l1.cpu()) < 1e-6

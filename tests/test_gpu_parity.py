@@ -15,7 +15,10 @@ from vmbd_gb300 import geometry, synth
 
 pytestmark = pytest.mark.gpu
 TOL = 1e-5
-GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "ref_*.npz")))
+_ALL = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "ref_*.npz")))
+# operator fixtures (cnv / cnvtp) and Fourier-division deconvolution fixtures
+GOLDEN = [p for p in _ALL if not os.path.basename(p).startswith("ref_deconv_")]
+DECONV_GOLDEN = [p for p in _ALL if os.path.basename(p).startswith("ref_deconv_")]
 
 
 def rel(a, b, mask=None):
@@ -76,15 +79,26 @@ CASES = {
     "cfg1_winaux": dict(sx=(256, 256), csf=(4, 4), sf=(15, 15)),
     # 512^2, 8x8 grid of 96^2 patches, 31^2 motion PSFs, frame 128
     "cfg2_literal": dict(sx=(512, 512), csf=(8, 8), sf=(31, 31), sw=(96, 96), hop=(48, 48), kind="motion"),
-    # 512^2, 8x8 winaux geometry (sw 122), frame 256
+    # 512^2, 8x8 winaux geometry (sw 122, E 152), frame 256
     "cfg2_winaux": dict(sx=(512, 512), csf=(8, 8), sf=(31, 31), kind="motion"),
+    # the same geometry on the 192 frame (24 x 8 mixed radix)
+    "cfg2_winaux_f192": dict(sx=(512, 512), csf=(8, 8), sf=(31, 31), kind="motion", sfft=192),
     # 512^2 frame of the MFBD workload, 25^2 PSFs, sw 120, frame 256
     "cfg3_winaux": dict(sx=(536, 536), csf=(8, 8), sf=(25, 25), kind="motion"),
-    # 384x512 member of the uneven batch: mixed-parity sw (116, 119)
+    "cfg3_winaux_f192": dict(sx=(536, 536), csf=(8, 8), sf=(25, 25), kind="motion", sfft=192),
+    # 384x512 member of the uneven batch: mixed-parity sw (116, 119), frame 256
     "cfg4_mixed": dict(sx=(404, 532), csf=(6, 8), sf=(21, 21), kind="motion"),
+    "cfg4_mixed_f192": dict(sx=(404, 532), csf=(6, 8), sf=(21, 21), kind="motion", sfft=192),
+    # a small geometry forced onto the 192 frame (zero padding well past E)
+    "cfg1_literal_f192": dict(sx=(256, 256), csf=(4, 4), sf=(15, 15), sw=(64, 64), hop=(32, 32), sfft=192),
     "same_mode": dict(sx=(200, 232), csf=(3, 4), sf=(12, 10), mode="same"),
     "full_mode": dict(sx=(200, 232), csf=(3, 4), sf=(12, 10), mode="full"),
+    "full_mode_f192": dict(sx=(200, 232), csf=(3, 4), sf=(12, 10), mode="full", sfft=192),
 }
+# frame each case runs on
+FRAME = {"cfg1_literal": 128, "cfg1_winaux": 128, "cfg2_literal": 128, "cfg2_winaux": 256,
+         "cfg2_winaux_f192": 192, "cfg3_winaux": 256, "cfg3_winaux_f192": 192, "cfg4_mixed": 256,
+         "cfg4_mixed_f192": 192, "cfg1_literal_f192": 192}
 
 
 @pytest.fixture(params=[1, 2], ids=["cta", "cluster2"])
@@ -100,8 +114,12 @@ def cluster_mode(request, cuda):
 @pytest.mark.parametrize("name", list(CASES))
 def test_operator_matches_fp64_oracle(cuda, cluster_mode, name):
     from vmbd_gb300.eff import EffPlan
-    wa, g, x, f, r = make(**CASES[name])
-    plan = EffPlan(wa, g.sf, g.mode, device=cuda)
+    spec = dict(CASES[name])
+    sfft = spec.pop("sfft", 0)
+    wa, g, x, f, r = make(**spec)
+    plan = EffPlan(wa, g.sf, g.mode, sfft=sfft, device=cuda)
+    if name in FRAME:
+        assert plan.N == FRAME[name]
     ws = wa.ws.astype(np.float64)
     fh = plan.psf_spectrum(t(f, cuda))
     xh_fwd = plan.empty_spectrum()

@@ -10,7 +10,10 @@ import pytest
 from oracle import eff64
 from vmbd_gb300 import geometry, synth
 
-GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "ref_*.npz")))
+_ALL = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "ref_*.npz")))
+# operator fixtures (cnv / cnvtp) and Fourier-division deconvolution fixtures
+GOLDEN = [p for p in _ALL if not os.path.basename(p).startswith("ref_deconv_")]
+DECONV_GOLDEN = [p for p in _ALL if os.path.basename(p).startswith("ref_deconv_")]
 
 
 def load_case(path):
@@ -59,6 +62,58 @@ def test_oracle_matches_reference_adjoints(path):
     m = np.isfinite(c["gx"])
     assert rel(gx, c["gx"], m) < 2e-6
     assert rel(gf, c["gf"]) < 2e-6
+
+
+@pytest.mark.parametrize("path", DECONV_GOLDEN, ids=lambda p: os.path.basename(p))
+def test_oracle_matches_reference_xdirect(path):
+    """OlaGPU.deconv(mode='xdirect') of an F object (image estimate) and of
+    an X object (PSF estimate), the reference run on its own kernels; the
+    reference frame (``sfft``) is the one the division happens in."""
+    z = np.load(path)
+    c = {k: z[k] for k in z.files}
+    g = eff64.Geometry(tuple(c["sx"]), tuple(c["sf"]), tuple(c["csf"]), tuple(c["sw"]), tuple(c["hop"]),
+                       str(c["mode"]), tuple(c["sfft"]))
+    ws = c["ws"].astype(np.float64)
+    alpha, beta = float(c["alpha"]), float(c["beta"])
+    u = eff64.deconv_xdirect(c["y"], eff64.psf_spectrum(c["f"], g), g, ws, "image", alpha, beta)
+    fz = eff64.deconv_xdirect(c["y"], eff64.image_spectrum(c["x"], g, ws), g, ws, "psf", alpha, beta)
+    assert rel(u, c["u"]) < 2e-6
+    assert rel(fz, c["fz"]) < 1e-5
+
+
+def test_deconv_golden_present():
+    assert len(DECONV_GOLDEN) >= 3
+
+
+def test_xdirect_with_delta_psfs_returns_the_image():
+    """Known answer: PSFs that are deltas at the origin have spectrum 1, so
+    the division is a scaling by 1/(1 + beta) and the image estimate at pixel
+    i is the overlap-add of ws_k[i - m*hop] * y[i - (sf-1)] over the patches
+    whose chop (frame rows [sf-1, sw)) reaches i.  Where every covering patch
+    reaches it, that sum is y[i - (sf-1)] = x[i] (partition of unity)."""
+    wa = geometry.win2winaux((64, 64), (2, 2), 0.5)
+    sf = (5, 5)
+    g = eff64.Geometry(wa.sx, sf, wa.csf, wa.sw, wa.nhop, "valid")
+    ws = wa.ws.astype(np.float64)
+    x = synth.blob_edge_image(wa.sx, seed=3)
+    f = np.zeros((g.K,) + sf)
+    f[:, 0, 0] = 1.0
+    y = eff64.forward(x, f, g, ws)
+    beta = 1e-3
+    u = eff64.deconv_xdirect(y, eff64.psf_spectrum(f, g), g, ws, "image", 0.0, beta)
+    ok = []
+    for d in range(2):
+        i = np.arange(wa.sx[d])
+        good = np.ones(wa.sx[d], bool)
+        for m in range(wa.csf[d]):
+            r = i - m * wa.nhop[d]
+            covered = (r >= 0) & (r < wa.sw[d])
+            good &= ~covered | (r >= sf[d] - 1)
+        ok.append(good)
+    mask = ok[0][:, None] & ok[1][None, :]
+    assert mask.sum() > 0.5 * mask.size
+    # the window stack is float32: its partition of unity holds to ~1e-7
+    assert np.abs(u[mask] - x[mask] / (1 + beta)).max() < 1e-6
 
 
 @pytest.mark.parametrize("path", GOLDEN, ids=lambda p: os.path.basename(p))

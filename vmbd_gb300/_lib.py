@@ -30,14 +30,14 @@ EXPORTS = (
     "eff_static_scratch_bytes", "eff_loss_grad_static", "eff_edgetaper",
     "eff_adjoint_masked", "eff_dots3", "eff_pg_step", "eff_mu_update", "eff_max_nonneg",
     "eff_set_cluster_mode", "eff_batch_create", "eff_batch_destroy", "eff_batch_items",
-    "eff_batch_forward_both", "eff_batch_adjoint_residual",
+    "eff_batch_forward_both", "eff_batch_adjoint_residual", "eff_deconv_xdirect",
 )
 
 
 class EffGeom(ctypes.Structure):
     _fields_ = [("sx", ctypes.c_int * 2), ("sf", ctypes.c_int * 2), ("csf", ctypes.c_int * 2),
                 ("sw", ctypes.c_int * 2), ("hop", ctypes.c_int * 2), ("sfft", ctypes.c_int),
-                ("mode", ctypes.c_int)]
+                ("mode", ctypes.c_int), ("threads", ctypes.c_int)]
 
 
 class EffError(RuntimeError):
@@ -95,6 +95,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "eff_batch_adjoint_residual": ([vp, vp, vp, vp, vp, vp, vp, vp, vp], ip),
         "eff_mu_update": ([fp, fp, fp, ctypes.c_float, ip, ip, ip, ip, vp, ctypes.c_float, vp, vp], ip),
         "eff_loss_grad_static": ([vp, fp, fp, fp, vp, fp, fp, ip, vp], ip),
+        "eff_deconv_xdirect": ([vp, fp, vp, vp, fp, fp, ctypes.c_float, ctypes.c_float, ip, vp], ip),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)

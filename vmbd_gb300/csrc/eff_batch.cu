@@ -37,6 +37,14 @@ struct Item {
   int cls, b, k, pad;
 };
 
+// One patch of one frame size as a separate (not inlined) function: the
+// persistent kernel calls one per item, and each is register-allocated and
+// compiled on its own instead of as one very large kernel body.
+template <int N, int OP>
+__device__ __noinline__ void batch_patch(const Params& P, int k, long long b, float2* smem, int cta, int ncta) {
+  eff_patch<N, OP, 2>(P, k, b, smem, cta, ncta);
+}
+
 template <int OP>
 __global__ void __launch_bounds__(kBatchThreads) eff_persistent(const ClassTable T, const Item* __restrict__ items,
                                                                 int n_items) {
@@ -48,9 +56,10 @@ __global__ void __launch_bounds__(kBatchThreads) eff_persistent(const ClassTable
     const Params& P = T.P[it.cls];
     const int K = P.csf0 * P.csf1;
     switch (T.N[it.cls]) {
-      case 256: eff_patch<256, OP, 2>(P, it.k, it.b, smem, 2 * it.k + rank, 2 * K); break;
-      case 128: eff_patch<128, OP, 2>(P, it.k, it.b, smem, 2 * it.k + rank, 2 * K); break;
-      default: eff_patch<64, OP, 2>(P, it.k, it.b, smem, 2 * it.k + rank, 2 * K); break;
+      case 256: batch_patch<256, OP>(P, it.k, it.b, smem, 2 * it.k + rank, 2 * K); break;
+      case 192: batch_patch<192, OP>(P, it.k, it.b, smem, 2 * it.k + rank, 2 * K); break;
+      case 128: batch_patch<128, OP>(P, it.k, it.b, smem, 2 * it.k + rank, 2 * K); break;
+      default: batch_patch<64, OP>(P, it.k, it.b, smem, 2 * it.k + rank, 2 * K); break;
     }
   }
 }

@@ -47,7 +47,8 @@ struct EffPlan {
   int device;
   float2* win0;
   float2* win1;
-  float2* tw;
+  float2* tw;   // twiddle table [N], followed in the same allocation by
+  float* lap;   // the difference-filter spectrum 4 sin^2(pi k / N) [N]
 };
 
 namespace {
@@ -66,7 +67,13 @@ int cuda_fail(cudaError_t e, const char* what) {
   return fail(EFF_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-int frame_ok(int n) { return n == 64 || n == 128 || n == 256; }
+// Frame edges chosen automatically (ascending): the powers of two.  The
+// 192 frame (24 x 8 mixed radix) is compiled too but only used on request:
+// its 24 values per lane make each lane's dependent chain ~1.5x longer, which
+// costs more than its ~45% less arithmetic saves on latency-bound single
+// images; batches that fill the GPU can gain (the batch autotuner tries it).
+constexpr int kFrames[] = {64, 128, 256};
+int frame_ok(int n) { return n == 64 || n == 128 || n == 192 || n == 256; }
 
 eff::Params base_params(const EffPlan* p) {
   eff::Params P;
@@ -84,6 +91,7 @@ eff::Params base_params(const EffPlan* p) {
   P.win0 = p->win0;
   P.win1 = p->win1;
   P.tw = p->tw;
+  P.lap = p->lap;
   P.x_bs = (long long)g.sx[0] * g.sx[1];
   P.f_bs = (long long)p->K * g.sf[0] * g.sf[1];
   P.y_bs = (long long)p->sy[0] * p->sy[1];
@@ -111,6 +119,7 @@ int run(const EffPlan* p, int op, const eff::Params& P, int batch, void* stream)
   switch (p->N) {
     case 64: e = eff::launch_n64(op, CL, P, p->K, batch, threads, smem, st); break;
     case 128: e = eff::launch_n128(op, CL, P, p->K, batch, threads, smem, st); break;
+    case 192: e = eff::launch_n192(op, CL, P, p->K, batch, threads, smem, st); break;
     case 256: e = eff::launch_n256(op, CL, P, p->K, batch, threads, smem, st); break;
     default: return fail(EFF_ERR_UNSUPPORTED, "frame size");
   }
@@ -253,21 +262,28 @@ int eff_plan_create(const EffGeom* geom, const float* win0, const float* win1, E
   }
   const int emax = p.E[0] > p.E[1] ? p.E[0] : p.E[1];
   if (g.sfft == 0) {
-    int n = 64;
-    while (n < emax) n <<= 1;
-    p.N = n;
+    p.N = 0;
+    for (int n : kFrames)
+      if (n >= emax) {
+        p.N = n;
+        break;
+      }
+    if (p.N == 0) p.N = 512;  // rejected below
   } else {
     p.N = g.sfft;
   }
   if (!frame_ok(p.N))
     return fail(EFF_ERR_UNSUPPORTED, "FFT frame " + std::to_string(p.N) +
-                                         " (needs a power of two in [64, 256] >= sw + sf - 1 = " +
+                                         " (needs 64, 128, 192 or 256, >= sw + sf - 1 = " +
                                          std::to_string(emax) + ")");
   if (p.N < emax) return fail(EFF_ERR_INVALID, "FFT frame smaller than sw + sf - 1");
+  if (g.threads != 0 && (g.threads < 32 || g.threads % 32 != 0 || g.threads > eff::max_threads(p.N)))
+    return fail(EFF_ERR_INVALID, "threads must be 0 or a multiple of 32 in [32, " +
+                                     std::to_string(eff::max_threads(p.N)) + "]");
 
   // Threads per CTA: the most the kernels are compiled for, halved while the
   // frame plus the per-group exchange scratch would not fit in shared memory.
-  p.threads = eff::max_threads(p.N);
+  p.threads = g.threads ? g.threads : eff::max_threads(p.N);
   {
     eff::Params P = base_params(&p);
     P.out0 = reinterpret_cast<float*>(1);
@@ -279,12 +295,13 @@ int eff_plan_create(const EffGeom* geom, const float* win0, const float* win1, E
         if (s > worst) worst = s;
       }
       if (worst <= kSmemLimit || p.threads <= 128) break;
-      p.threads /= 2;
+      p.threads = (p.threads / 2 + 31) / 32 * 32;
     }
     // 2-CTA clusters: one lane group per column unit a CTA owns (N/4 units
-    // of N/16 lanes), at most the compiled maximum, halved while the frame
+    // of G = N/R lanes), at most the compiled maximum, halved while the frame
     // half plus the exchange scratch does not fit.
-    p.threads2 = std::min(eff::max_threads(p.N), std::max(128, p.N * p.N / 64));
+    p.threads2 = g.threads ? g.threads
+                           : std::min(eff::max_threads(p.N), std::max(128, p.N / 4 * (p.N / eff::lane_values(p.N))));
     for (;;) {
       size_t worst = 0;
       for (int op = 0; op < eff::kNumOps; ++op) {
@@ -292,7 +309,7 @@ int eff_plan_create(const EffGeom* geom, const float* win0, const float* win1, E
         if (s > worst) worst = s;
       }
       if (worst <= kSmemLimit || p.threads2 <= 128) break;
-      p.threads2 /= 2;
+      p.threads2 = (p.threads2 / 2 + 31) / 32 * 32;
     }
   }
 
@@ -302,15 +319,24 @@ int eff_plan_create(const EffGeom* geom, const float* win0, const float* win1, E
   if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceGetAttribute");
 
   // Twiddle table [k1*G + g] = exp(-2 pi i g k1 / N), FP64 then rounded.
-  const int G = p.N / 16;
+  const int R = eff::lane_values(p.N), G = p.N / R;
   std::vector<float2> tw(p.N);
-  for (int k1 = 0; k1 < 16; ++k1)
+  for (int k1 = 0; k1 < R; ++k1)
     for (int gg = 0; gg < G; ++gg) {
       const double a = -2.0 * M_PI * double(gg * k1) / double(p.N);
       tw[k1 * G + gg] = make_float2((float)std::cos(a), (float)std::sin(a));
     }
+  // |FFT([-1, 1])|^2 on N points = 4 sin^2(pi k / N), FP64 then rounded
+  // (the Laplacian term of deconv 'xdirect', olaGPU.py:553-561).
+  std::vector<float> lap(p.N);
+  for (int k = 0; k < p.N; ++k) {
+    const double s = std::sin(M_PI * double(k) / double(p.N));
+    lap[k] = (float)(4.0 * s * s);
+  }
   const size_t n0 = 2 * (size_t)g.csf[0] * g.sw[0], n1 = 2 * (size_t)g.csf[1] * g.sw[1];
-  if ((e = cudaMalloc(&p.tw, sizeof(float2) * p.N)) != cudaSuccess) return cuda_fail(e, "cudaMalloc");
+  if ((e = cudaMalloc(&p.tw, (sizeof(float2) + sizeof(float)) * p.N)) != cudaSuccess)
+    return cuda_fail(e, "cudaMalloc");
+  p.lap = reinterpret_cast<float*>(p.tw + p.N);
   if ((e = cudaMalloc(&p.win0, sizeof(float) * n0)) != cudaSuccess) {
     cudaFree(p.tw);
     return cuda_fail(e, "cudaMalloc");
@@ -321,6 +347,7 @@ int eff_plan_create(const EffGeom* geom, const float* win0, const float* win1, E
     return cuda_fail(e, "cudaMalloc");
   }
   if ((e = cudaMemcpy(p.tw, tw.data(), sizeof(float2) * p.N, cudaMemcpyHostToDevice)) != cudaSuccess ||
+      (e = cudaMemcpy(p.lap, lap.data(), sizeof(float) * p.N, cudaMemcpyHostToDevice)) != cudaSuccess ||
       (e = cudaMemcpy(p.win0, win0, sizeof(float) * n0, cudaMemcpyHostToDevice)) != cudaSuccess ||
       (e = cudaMemcpy(p.win1, win1, sizeof(float) * n1, cudaMemcpyHostToDevice)) != cudaSuccess) {
     cudaFree(p.tw);
@@ -417,6 +444,35 @@ int eff_adjoint_residual(const EffPlan* plan, const float* y, const float* y_obs
                          int batch, void* stream) {
   if (!y_obs) return fail(EFF_ERR_INVALID, "null y_obs");
   return adjoint_impl(plan, y, y_obs, fhat, xhat, gx, gf, loss, adj_mode, batch, stream);
+}
+
+int eff_deconv_xdirect(const EffPlan* plan, const float* y, const void* fhat, const void* xhat, float* u,
+                       float* fz, float alpha, float beta, int batch, void* stream) {
+  if (int s = check_plan(plan, batch)) return s;
+  if (!y || (!u && !fz)) return fail(EFF_ERR_INVALID, "null argument");
+  if (u && !fhat) return fail(EFF_ERR_INVALID, "image estimate needs the PSF spectrum");
+  if (fz && !xhat) return fail(EFF_ERR_INVALID, "PSF estimate needs the image spectrum");
+  if (plan->g.mode == EFF_MODE_FULL) return fail(EFF_ERR_UNSUPPORTED, "Not a valid mode!");  // olaGPU.py:570-571
+  if (!(alpha >= 0.f) || !(beta >= 0.f)) return fail(EFF_ERR_INVALID, "alpha and beta must be >= 0");
+  eff::Params P = base_params(plan);
+  P.y = y;
+  P.b0 = static_cast<const float2*>(fhat);
+  P.b1 = static_cast<const float2*>(xhat);
+  P.out0 = u;
+  P.out1 = fz;
+  P.out0_bs = P.x_bs;
+  P.out1_bs = P.f_bs;
+  // the chop of y sits at frame offset `off` (sf - 1 valid, floor(sf/2) same)
+  P.lo0 = plan->off[0];
+  P.lo1 = plan->off[1];
+  P.alpha = alpha;
+  P.beta = beta;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (u) {
+    cudaError_t e = cudaMemsetAsync(u, 0, sizeof(float) * P.x_bs * batch, st);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+  }
+  return run(plan, eff::OP_DECONV, P, batch, stream);
 }
 
 int eff_adjoint_masked(const EffPlan* plan, const float* y, const float* mask, const void* fhat,

@@ -1,19 +1,20 @@
 // Register / sub-warp FFT building blocks for the EFF kernels (sm_103a).
 //
-// A length-N complex FFT (N = 16*G, G in {4, 8, 16}) is computed by a group of
-// G consecutive lanes of one warp, each lane holding 16 values:
+// A length-N complex FFT (N = R*G: N = 64, 128, 256 with R = 16 values per
+// lane; N = 192 with R = 24) is computed by a group of G consecutive lanes of
+// one warp, each lane holding R values:
 //
 //   layout "A": lane g, register m  <->  element g + G*m.
 //
-// Forward:  16-point DFT in registers over m, twiddle by W_N^{g*k1}, exchange
+// Forward:  R-point DFT in registers over m, twiddle by W_N^{g*k1}, exchange
 // through a per-group shared-memory scratch so that lane g owns k1 = g + G*t
-// (t < 16/G), then G-point DFTs in registers.  The result is again in layout
+// (t < R/G), then G-point DFTs in registers.  The result is again in layout
 // A (register j holds X[g + G*j]), so FFT -> pointwise product -> inverse FFT
 // needs no reordering.  The inverse runs the same steps backwards with
 // conjugate twiddles (unnormalised).
 //
 // Arithmetic is FP32; the in-register twiddles are exact decimal expansions of
-// cos/sin(2*pi*j/16) and the W_N table is computed in FP64 on the host.
+// cos/sin(2*pi*j/48) and the W_N table is computed in FP64 on the host.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -31,27 +32,39 @@ __device__ __forceinline__ float2 cmulc(float2 a, float2 b) {
 }
 __device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
 
-// cos / sin of 2*pi*j/16.
-__host__ __device__ constexpr float cos16(int j) {
-  constexpr float C1 = 0.92387953251128674f, S1 = 0.38268343236508978f, H = 0.70710678118654752f;
-  switch (j & 15) {
-    case 0: return 1.f;   case 1: return C1;   case 2: return H;    case 3: return S1;
-    case 4: return 0.f;   case 5: return -S1;  case 6: return -H;   case 7: return -C1;
-    case 8: return -1.f;  case 9: return -C1;  case 10: return -H;  case 11: return -S1;
-    case 12: return 0.f;  case 13: return S1;  case 14: return H;   default: return C1;
+// cos / sin of 2*pi*j/48.
+__host__ __device__ constexpr float cos48_q(int j) {  // j in [0, 12]
+  switch (j) {
+    case 0: return 1.f;
+    case 1: return 0.99144486137381041f;
+    case 2: return 0.96592582628906829f;
+    case 3: return 0.92387953251128674f;
+    case 4: return 0.86602540378443865f;
+    case 5: return 0.79335334029123517f;
+    case 6: return 0.70710678118654752f;
+    case 7: return 0.60876142900872066f;
+    case 8: return 0.5f;
+    case 9: return 0.38268343236508978f;
+    case 10: return 0.25881904510252076f;
+    case 11: return 0.13052619222005159f;
+    default: return 0.f;
   }
 }
-__host__ __device__ constexpr float sin16(int j) { return cos16(j - 4); }
+__host__ __device__ constexpr float cos48(int j) {
+  j = ((j % 48) + 48) % 48;
+  return j <= 12 ? cos48_q(j) : (j <= 24 ? -cos48_q(24 - j) : (j <= 36 ? -cos48_q(j - 24) : cos48_q(48 - j)));
+}
+__host__ __device__ constexpr float sin48(int j) { return cos48(j - 12); }
 
-// v * W where W = exp(-+ 2*pi*i * e16/16) (forward: minus, INV: plus).
+// v * W where W = exp(-+ 2*pi*i * e48/48) (forward: minus, INV: plus).
 template <bool INV>
-__device__ __forceinline__ float2 twiddle16(float2 v, int e16) {
-  e16 &= 15;
-  if (e16 == 0) return v;
-  if (e16 == 8) return make_float2(-v.x, -v.y);
-  if (e16 == 4) return INV ? make_float2(-v.y, v.x) : make_float2(v.y, -v.x);
-  if (e16 == 12) return INV ? make_float2(v.y, -v.x) : make_float2(-v.y, v.x);
-  const float c = cos16(e16), s = sin16(e16);
+__device__ __forceinline__ float2 twiddle48(float2 v, int e48) {
+  e48 = ((e48 % 48) + 48) % 48;
+  if (e48 == 0) return v;
+  if (e48 == 24) return make_float2(-v.x, -v.y);
+  if (e48 == 12) return INV ? make_float2(-v.y, v.x) : make_float2(v.y, -v.x);
+  if (e48 == 36) return INV ? make_float2(v.y, -v.x) : make_float2(-v.y, v.x);
+  const float c = cos48(e48), s = sin48(e48);
   if (INV) return make_float2(fmaf(v.x, c, -v.y * s), fmaf(v.y, c, v.x * s));
   return make_float2(fmaf(v.x, c, v.y * s), fmaf(v.y, c, -v.x * s));
 }
@@ -65,11 +78,11 @@ __host__ __device__ constexpr int bitrev(int i, int R) {
   return r;
 }
 
-// In-register DFT of size R (2..16), natural order in and out.
-// Iterative radix-2 decimation in time; every index is a compile-time
+// In-register DFT of a power-of-two size R (2..16), natural order in and
+// out: iterative radix-2 decimation in time; every index is a compile-time
 // constant after unrolling, so the bit reversal is register renaming.
 template <int R, bool INV>
-__device__ __forceinline__ void dft(float2 (&a)[R]) {
+__device__ __forceinline__ void dft_pow2(float2 (&a)[R]) {
   float2 b[R];
 #pragma unroll
   for (int i = 0; i < R; ++i) b[bitrev(i, R)] = a[i];
@@ -80,7 +93,7 @@ __device__ __forceinline__ void dft(float2 (&a)[R]) {
 #pragma unroll
       for (int j = 0; j < len / 2; ++j) {
         const float2 u = b[i + j];
-        const float2 v = twiddle16<INV>(b[i + j + len / 2], j * (16 / len));
+        const float2 v = twiddle48<INV>(b[i + j + len / 2], j * (48 / len));
         b[i + j] = cadd(u, v);
         b[i + j + len / 2] = csub(u, v);
       }
@@ -90,28 +103,72 @@ __device__ __forceinline__ void dft(float2 (&a)[R]) {
   for (int i = 0; i < R; ++i) a[i] = b[i];
 }
 
+// 3-point DFT of (a, b, c) in place.
+template <bool INV>
+__device__ __forceinline__ void dft3(float2& a, float2& b, float2& c) {
+  constexpr float S = 0.86602540378443865f;  // sqrt(3)/2
+  const float2 t1 = cadd(b, c), t2 = csub(b, c);
+  const float2 m = make_float2(fmaf(-0.5f, t1.x, a.x), fmaf(-0.5f, t1.y, a.y));
+  a = cadd(a, t1);
+  // forward: X1 = m - i S t2, X2 = m + i S t2 (inverse: the conjugate)
+  const float2 n = INV ? make_float2(-S * t2.y, S * t2.x) : make_float2(S * t2.y, -S * t2.x);
+  b = cadd(m, n);
+  c = csub(m, n);
+}
+
+// 24-point DFT: n = 8*n1 + n2, k = k1 + 3*k2 -- DFT-3 over n1 for each n2,
+// twiddle W_24^{n2*k1}, DFT-8 over n2 for each k1.
+template <bool INV>
+__device__ __forceinline__ void dft24(float2 (&a)[24]) {
+  float2 y[3][8];
+#pragma unroll
+  for (int n2 = 0; n2 < 8; ++n2) {
+    float2 p = a[n2], q = a[8 + n2], r = a[16 + n2];
+    dft3<INV>(p, q, r);
+    y[0][n2] = p;
+    y[1][n2] = twiddle48<INV>(q, 2 * n2);      // W_24^{n2}
+    y[2][n2] = twiddle48<INV>(r, 2 * 2 * n2);  // W_24^{2 n2}
+  }
+#pragma unroll
+  for (int k1 = 0; k1 < 3; ++k1) {
+    dft_pow2<8, INV>(y[k1]);
+#pragma unroll
+    for (int k2 = 0; k2 < 8; ++k2) a[k1 + 3 * k2] = y[k1][k2];
+  }
+}
+
+template <int R, bool INV>
+__device__ __forceinline__ void dft(float2 (&a)[R]) {
+  if constexpr (R == 24) dft24<INV>(a);
+  else dft_pow2<R, INV>(a);
+}
+
+// Values each lane holds for a length-N transform.
+__host__ __device__ constexpr int lane_values(int N) { return N % 3 == 0 ? 24 : 16; }
+
 template <int N>
 struct FftShape {
-  static constexpr int R = 16;          // values per lane
-  static constexpr int G = N / 16;      // lanes per transform
-  static constexpr int T = R / G;       // k1 values per lane after the exchange
-  static constexpr int PAD = 1;         // scratch row padding (bank spread)
-  static constexpr int SCR = R * (G + PAD) + 8;  // float2 per group scratch (+8: group offset)
-  static_assert(G >= 2 && G <= 16 && (R % G) == 0, "supported N: 32..256");
+  static constexpr int R = lane_values(N);          // values per lane
+  static constexpr int G = N / R;                    // lanes per transform
+  static constexpr int T = R / G;                    // k1 values per lane after the exchange
+  static constexpr int PAD = 1;                      // scratch row padding (bank spread)
+  static constexpr int SCR = R * (G + PAD) + 8;      // float2 per group scratch (+8: group offset)
+  static_assert(G >= 2 && G <= 16 && (R % G) == 0 && (G & (G - 1)) == 0, "supported N: 32..256, 192");
 };
 
 // Forward FFT of length N over a lane group: v in layout A (natural), out in
 // layout A (natural).  tw: table [k1*G + g] = W_N^{g*k1}.  scr: this group's
 // scratch (FftShape<N>::SCR float2).  mask: the group's lanes.
 template <int N>
-__device__ __forceinline__ void fft_fwd(float2 (&v)[16], int g, float2* scr, const float2* tw,
+__device__ __forceinline__ void fft_fwd(float2 (&v)[FftShape<N>::R], int g, float2* scr, const float2* tw,
                                         unsigned mask) {
   using S = FftShape<N>;
-  dft<16, false>(v);
+  constexpr int R = S::R;
+  dft<R, false>(v);
 #pragma unroll
-  for (int k1 = 1; k1 < 16; ++k1) v[k1] = cmul(v[k1], tw[k1 * S::G + g]);
+  for (int k1 = 1; k1 < R; ++k1) v[k1] = cmul(v[k1], tw[k1 * S::G + g]);
 #pragma unroll
-  for (int k1 = 0; k1 < 16; ++k1) scr[k1 * (S::G + S::PAD) + g] = v[k1];
+  for (int k1 = 0; k1 < R; ++k1) scr[k1 * (S::G + S::PAD) + g] = v[k1];
   __syncwarp(mask);
 #pragma unroll
   for (int t = 0; t < S::T; ++t) {
@@ -128,9 +185,10 @@ __device__ __forceinline__ void fft_fwd(float2 (&v)[16], int g, float2* scr, con
 
 // Inverse (unnormalised) FFT: v in layout A (natural frequency), out layout A.
 template <int N>
-__device__ __forceinline__ void fft_inv(float2 (&v)[16], int g, float2* scr, const float2* tw,
+__device__ __forceinline__ void fft_inv(float2 (&v)[FftShape<N>::R], int g, float2* scr, const float2* tw,
                                         unsigned mask) {
   using S = FftShape<N>;
+  constexpr int R = S::R;
 #pragma unroll
   for (int t = 0; t < S::T; ++t) {
     float2 w[S::G];
@@ -143,26 +201,27 @@ __device__ __forceinline__ void fft_inv(float2 (&v)[16], int g, float2* scr, con
   }
   __syncwarp(mask);
 #pragma unroll
-  for (int k1 = 0; k1 < 16; ++k1) v[k1] = scr[k1 * (S::G + S::PAD) + g];
+  for (int k1 = 0; k1 < R; ++k1) v[k1] = scr[k1 * (S::G + S::PAD) + g];
   __syncwarp(mask);
 #pragma unroll
-  for (int k1 = 1; k1 < 16; ++k1) v[k1] = cmulc(v[k1], tw[k1 * S::G + g]);
-  dft<16, true>(v);
+  for (int k1 = 1; k1 < R; ++k1) v[k1] = cmulc(v[k1], tw[k1 * S::G + g]);
+  dft<R, true>(v);
 }
 
 // Value of register j's Hermitian partner: X[N - (g + G*j)] from the lane
-// that holds it (lane G-g, register 15-j; lane 0 pairs with itself).
+// that holds it (lane G-g, register R-1-j; lane 0 pairs with itself).
 template <int N>
-__device__ __forceinline__ void hermitian_partner(const float2 (&v)[16], float2 (&p)[16], int g,
-                                                  unsigned mask) {
+__device__ __forceinline__ void hermitian_partner(const float2 (&v)[FftShape<N>::R], float2 (&p)[FftShape<N>::R],
+                                                  int g, unsigned mask) {
   using S = FftShape<N>;
+  constexpr int R = S::R;
   const int src = (S::G - g) & (S::G - 1);
 #pragma unroll
-  for (int j = 0; j < 16; ++j) {
-    const float2 s = v[15 - j];
+  for (int j = 0; j < R; ++j) {
+    const float2 s = v[R - 1 - j];
     const float px = __shfl_sync(mask, s.x, src, S::G);
     const float py = __shfl_sync(mask, s.y, src, S::G);
-    p[j] = (g == 0) ? v[(16 - j) & 15] : make_float2(px, py);
+    p[j] = (g == 0) ? v[(R - j) % R] : make_float2(px, py);
   }
 }
 

@@ -1,7 +1,7 @@
 // Fused EFF kernels: one CTA per patch (blockIdx.x) and image (blockIdx.y).
 //
-// Every kernel runs the same three phases over an N x N frame (N = 64/128/256,
-// a power of two >= sw + sf - 1 in both dims) held as a half spectrum
+// Every kernel runs the same three phases over an N x N frame (N = 64, 128,
+// 192 or 256, >= sw + sf - 1 in both dims) held as a half spectrum
 // (N/2+1 bins per row) in shared memory:
 //
 //  1. row pass (R2C): pairs of real operand rows are read straight from HBM
@@ -40,10 +40,11 @@ enum Op : int {
   OP_FWD_PSF = 3,     // y = X f, X given by X-hat (X.cnv(f), olaGPU.py:188-193, 219-257)
   OP_FWD_BOTH = 4,    // y = EFF(x, f) from raw x and f; leaves X-hat and F-hat behind
   OP_ADJ = 5,         // F^T r and/or X^T r (cnvtp, olaGPU.py:261-311), r = y or y - y_obs
+  OP_DECONV = 6,      // Fourier-division deconvolution of y (deconv 'xdirect', olaGPU.py:550-609)
 };
-constexpr int kNumOps = 6;
+constexpr int kNumOps = 7;
 
-enum Operand : int { OPND_IMAGE = 0, OPND_PSF = 1, OPND_RESID = 2 };
+enum Operand : int { OPND_IMAGE = 0, OPND_PSF = 1, OPND_RESID = 2, OPND_DCHOP = 3 };
 
 struct Params {
   int sx0, sx1, sf0, sf1, csf0, csf1, sw0, sw1, hop0, hop1;
@@ -63,10 +64,12 @@ struct Params {
   double* loss;            // adjoint with y_obs: += 0.5 * sum (y - y_obs)^2 (optional)
   const float2* win0;      // window factors (alpha, gamma) [csf0, sw0]
   const float2* win1;      // window factors (alpha, gamma) [csf1, sw1]
-  const float2* tw;        // W_N table [16*G]
+  const float2* tw;        // W_N table [R*G] = [N]
   long long x_bs, f_bs, y_bs, spec_bs, out0_bs, out1_bs;  // per-image strides
   const char* pf;          // forward: bytes [pf, pf + pf_bytes) to bring into L2 for the next kernel
   long long pf_bytes;
+  const float* lap;        // deconv: 4 sin^2(pi k / N), k < N (spectrum of the difference filters)
+  float alpha, beta;       // deconv: regularisation weights
 };
 
 // TMA bulk prefetch of a contiguous range into L2 (16-byte aligned start and
@@ -80,16 +83,18 @@ __device__ __forceinline__ void l2_prefetch_bulk(const void* p, unsigned bytes) 
 __host__ __device__ constexpr int frame_pitch(int N, int CL = 1) { return CL == 1 ? N / 2 + 1 : N / 4 + 1; }
 __host__ __device__ constexpr int even_up(int v) { return (v + 1) & ~1; }
 // Threads per CTA the kernel is compiled for (the host may launch fewer).
-__host__ __device__ constexpr int max_threads(int N) { return 512; }
+__host__ __device__ constexpr int max_threads(int N) { return N % 3 == 0 ? 384 : 512; }
 
 // Operand A / B of each op, their row counts and frame bases.
 __host__ __device__ constexpr int opnd_a(int op) {
-  return (op == OP_SPEC_PSF || op == OP_FWD_PSF) ? OPND_PSF : (op == OP_ADJ ? OPND_RESID : OPND_IMAGE);
+  return (op == OP_SPEC_PSF || op == OP_FWD_PSF)
+             ? OPND_PSF
+             : (op == OP_ADJ ? OPND_RESID : (op == OP_DECONV ? OPND_DCHOP : OPND_IMAGE));
 }
 __host__ __device__ constexpr bool has_b(int op) { return op == OP_FWD_BOTH; }
 
 __host__ __device__ inline int opnd_rows(const Params& P, int kind) {
-  return kind == OPND_IMAGE ? P.sw0 : (kind == OPND_PSF ? P.sf0 : P.E0);
+  return (kind == OPND_IMAGE || kind == OPND_DCHOP) ? P.sw0 : (kind == OPND_PSF ? P.sf0 : P.E0);
 }
 
 // Frame rows a CTA uses (the host sizes shared memory with the same formula).
@@ -161,6 +166,15 @@ __device__ __forceinline__ float operand(const Params& P, const Patch& T, int r,
   } else if constexpr (KIND == OPND_PSF) {
     if (r >= P.sf0 || c >= P.sf1) return 0.f;
     return __ldg(T.f + ((long long)T.k * P.sf0 + r) * P.sf1 + c);
+  } else if constexpr (KIND == OPND_DCHOP) {
+    // deconv 'xdirect': chop of y placed at frame offset lo (chop_pad_GPU,
+    // olaGPU.py:573-580) times the window stack at the frame origin
+    // (pad_stack_GPU(ws), :581-584); the supports overlap on [lo, sw)
+    if (r < P.lo0 || r >= P.sw0 || c < P.lo1 || c >= P.sw1) return 0.f;
+    const int i = T.m * P.hop0 + r - P.lo0, j = T.n * P.hop1 + c - P.lo1;
+    if (i >= P.sy0 || j >= P.sy1) return 0.f;
+    return window_weight(__ldg(P.win0 + T.m * P.sw0 + r), __ldg(P.win1 + T.n * P.sw1 + c)) *
+           __ldg(T.y + (long long)i * P.sy1 + j);
   } else {
     if (r < P.lo0 || r >= P.hi0 || c < P.lo1 || c >= P.hi1) return 0.f;
     const int i = T.m * P.hop0 + r - P.off0, j = T.n * P.hop1 + c - P.off1;
@@ -176,10 +190,11 @@ __device__ __forceinline__ float operand(const Params& P, const Patch& T, int r,
 // Operand rows (ra, ra+1) packed as re/im, layout A.
 template <int N, int KIND>
 __device__ __forceinline__ void load_rows(const Params& P, const Patch& T, int ra, int g,
-                                          float2 (&v)[16]) {
+                                          float2 (&v)[FftShape<N>::R]) {
   constexpr int G = FftShape<N>::G;
+  constexpr int R = FftShape<N>::R;
 #pragma unroll
-  for (int mm = 0; mm < 16; ++mm) {
+  for (int mm = 0; mm < R; ++mm) {
     const int c = g + G * mm;
     v[mm] = make_float2(operand<KIND>(P, T, ra, c), operand<KIND>(P, T, ra + 1, c));
   }
@@ -188,20 +203,21 @@ __device__ __forceinline__ void load_rows(const Params& P, const Patch& T, int r
 // R2C of one pair of rows already in v (layout A) into frame rows row,
 // row+1 (bins go to the CTA that owns their column).
 template <int N, int CL>
-__device__ __forceinline__ void r2c_store(float2 (&v)[16], const Frame<N, CL>& F, int row, float2* scr,
+__device__ __forceinline__ void r2c_store(float2 (&v)[FftShape<N>::R], const Frame<N, CL>& F, int row, float2* scr,
                                           const float2* tw, int g, unsigned gmask) {
   constexpr int G = FftShape<N>::G;
+  constexpr int R = FftShape<N>::R;
   constexpr int HP = Frame<N, CL>::HP;
   fft_fwd<N>(v, g, scr, tw, gmask);
-  float2 p[16];
+  float2 p[R];
   hermitian_partner<N>(v, p, g, gmask);
 #pragma unroll
-  for (int j = 0; j <= 8; ++j) {
-    if (j == 8 && g != 0) break;
+  for (int j = 0; j <= R / 2; ++j) {
+    if (j == R / 2 && g != 0) break;
     const int kk = g + G * j;
-    // bins g + G*j: j < 4 (and the N/2 bin, j = 8) lie in the first quarter
-    float2* base = F.part[(CL == 1 || j < 4 || j == 8) ? 0 : CL - 1];
-    const int col = CL == 1 ? kk : (j == 8 ? Frame<N, CL>::Q : (j < 4 ? kk : kk - Frame<N, CL>::Q));
+    // bins g + G*j: j < R/4 (and the N/2 bin, j = R/2) lie in the first quarter
+    float2* base = F.part[(CL == 1 || j < R / 4 || j == R / 2) ? 0 : CL - 1];
+    const int col = CL == 1 ? kk : (j == R / 2 ? Frame<N, CL>::Q : (j < R / 4 ? kk : kk - Frame<N, CL>::Q));
     float2* rowa = base + row * HP + col;
     rowa[0] = make_float2(0.5f * (v[j].x + p[j].x), 0.5f * (v[j].y - p[j].y));
     rowa[HP] = make_float2(0.5f * (v[j].y + p[j].y), 0.5f * (p[j].x - v[j].x));
@@ -211,15 +227,16 @@ __device__ __forceinline__ void r2c_store(float2 (&v)[16], const Frame<N, CL>& F
 // C2R of frame rows (ra, ra+1); returns real row ra in .x, ra+1 in .y,
 // layout A (register m holds column g + G*m).
 template <int N, int CL>
-__device__ __forceinline__ void c2r_unit(const Frame<N, CL>& F, int ra, float2 (&v)[16], float2* scr,
+__device__ __forceinline__ void c2r_unit(const Frame<N, CL>& F, int ra, float2 (&v)[FftShape<N>::R], float2* scr,
                                          const float2* tw, int g, unsigned gmask) {
   constexpr int G = FftShape<N>::G;
+  constexpr int R = FftShape<N>::R;
   constexpr int HP = Frame<N, CL>::HP;
 #pragma unroll
-  for (int j = 0; j < 16; ++j) {
+  for (int j = 0; j < R; ++j) {
     const int kk = g + G * j;
     float2 ya, yb;
-    if (j < 8 || (j == 8 && g == 0)) {
+    if (j < R / 2 || (j == R / 2 && g == 0)) {
       const float2* pa = F.at(ra, kk);
       ya = pa[0];
       yb = pa[HP];
@@ -239,10 +256,11 @@ __device__ __forceinline__ void c2r_unit(const Frame<N, CL>& F, int ra, float2 (
 // [base, base+rows), frame pitch HP.
 template <int N, int HP>
 __device__ __forceinline__ void load_column(const float2* frame, int col, bool dc, int dcN, int base, int rows,
-                                            int g, float2 (&v)[16]) {
+                                            int g, float2 (&v)[FftShape<N>::R]) {
   constexpr int G = FftShape<N>::G;
+  constexpr int R = FftShape<N>::R;
 #pragma unroll
-  for (int mm = 0; mm < 16; ++mm) {
+  for (int mm = 0; mm < R; ++mm) {
     const int r = g + G * mm;
     if (r < rows) {
       const float2* row = frame + (base + r) * HP;
@@ -256,11 +274,12 @@ __device__ __forceinline__ void load_column(const float2* frame, int col, bool d
 // Inverse-transformed column to rows [base, base + even(rows)).
 template <int N, int HP>
 __device__ __forceinline__ void store_column(float2* frame, int col, bool dc, int dcN, int base, int rows,
-                                             int g, const float2 (&v)[16]) {
+                                             int g, const float2 (&v)[FftShape<N>::R]) {
   constexpr int G = FftShape<N>::G;
+  constexpr int R = FftShape<N>::R;
   const int rows_e = even_up(rows);
 #pragma unroll
-  for (int mm = 0; mm < 16; ++mm) {
+  for (int mm = 0; mm < R; ++mm) {
     const int r = g + G * mm;
     if (r < rows_e) {
       float2* row = frame + (base + r) * HP;
@@ -274,64 +293,109 @@ __device__ __forceinline__ void store_column(float2* frame, int col, bool dc, in
   }
 }
 
-// Column spectrum of a real-row-transformed operand.  u != 0: a[] is the
-// spectrum of column u.  u == 0: the packed transform of columns 0 and N/2 is
-// split into a[] (column 0) and b[] (column N/2).
-template <int N, int HP>
-__device__ __forceinline__ void column_spectrum(const float2* frame, int u, int col, int dcN, int base,
-                                                int rows, int g, float2* scr, const float2* tw,
-                                                unsigned gmask, float2 (&a)[16], float2 (&b)[16]) {
-  load_column<N, HP>(frame, col, u == 0, dcN, base, rows, g, a);
-  fft_fwd<N>(a, g, scr, tw, gmask);
-  if (u == 0) {
-    float2 p[16];
-    hermitian_partner<N>(a, p, g, gmask);
+// The DC column unit transforms columns 0 and N/2 (both real after the row
+// pass) packed as one complex column.  dc_split separates the packed
+// spectrum into column 0's (a) and column N/2's (b) and parks both in the
+// CTA's DC stash (2N float2, lane-private slots [j*G + g] and
+// [N + j*G + g]), so that no third register array is live in the column
+// pass.
+template <int N>
+__device__ __forceinline__ void dc_split(const float2 (&v)[FftShape<N>::R], float2* stash, int g, unsigned gmask) {
+  constexpr int G = FftShape<N>::G;
+  constexpr int R = FftShape<N>::R;
+  float2 p[R];
+  hermitian_partner<N>(v, p, g, gmask);
 #pragma unroll
-    for (int j = 0; j < 16; ++j) {
-      const float2 v = a[j];
-      a[j] = make_float2(0.5f * (v.x + p[j].x), 0.5f * (v.y - p[j].y));
-      b[j] = make_float2(0.5f * (v.y + p[j].y), 0.5f * (p[j].x - v.x));
+  for (int j = 0; j < R; ++j) {
+    stash[j * G + g] = make_float2(0.5f * (v[j].x + p[j].x), 0.5f * (v[j].y - p[j].y));
+    stash[N + j * G + g] = make_float2(0.5f * (v[j].y + p[j].y), 0.5f * (p[j].x - v[j].x));
+  }
+}
+
+// Spectrum of column unit u to the cached-spectrum layout [bin][N]: a for
+// u != 0, the DC stash's two columns for u == 0.
+template <int N>
+__device__ __forceinline__ void store_spectrum(float2* __restrict__ dst, int u, int g,
+                                               const float2 (&a)[FftShape<N>::R], const float2* stash) {
+  constexpr int G = FftShape<N>::G;
+  constexpr int R = FftShape<N>::R;
+  float2* c0 = dst + (long long)u * N;
+  if (u != 0) {
+#pragma unroll
+    for (int j = 0; j < R; ++j) c0[g + G * j] = a[j];
+  } else {
+    float2* cN = dst + (long long)(N / 2) * N;
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+      c0[g + G * j] = stash[j * G + g];
+      cN[g + G * j] = stash[N + j * G + g];
     }
   }
 }
 
-template <int N>
-__device__ __forceinline__ void store_spectrum(float2* __restrict__ dst, int u, int g,
-                                               const float2 (&a)[16], const float2 (&b)[16]) {
-  constexpr int G = FftShape<N>::G;
-  float2* c0 = dst + (long long)u * N;
-#pragma unroll
-  for (int j = 0; j < 16; ++j) c0[g + G * j] = a[j];
-  if (u == 0) {
-    float2* cN = dst + (long long)(N / 2) * N;
-#pragma unroll
-    for (int j = 0; j < 16; ++j) cN[g + G * j] = b[j];
-  }
-}
-
-// Product of the column spectrum (a, b) with a cached spectrum, packed for
-// one inverse transform (u == 0: column 0 product + i * column N/2 product).
+// Product of the column spectrum with a cached spectrum bh, packed for one
+// inverse transform: u != 0 from a; u == 0 from the DC stash, column 0
+// product + i * column N/2 product.  out may alias a.
 template <int N, bool CONJ>
-__device__ __forceinline__ void column_product(const float2 (&a)[16], const float2 (&b)[16],
+__device__ __forceinline__ void column_product(const float2 (&a)[FftShape<N>::R], const float2* stash,
                                                const float2* __restrict__ bh, int u, int g,
-                                               float scale, float2 (&out)[16]) {
+                                               float scale, float2 (&out)[FftShape<N>::R]) {
   constexpr int G = FftShape<N>::G;
+  constexpr int R = FftShape<N>::R;
   const float2* c0 = bh + (long long)u * N;
   if (u != 0) {
 #pragma unroll
-    for (int j = 0; j < 16; ++j) {
+    for (int j = 0; j < R; ++j) {
       const float2 s = __ldg(c0 + g + G * j);
       out[j] = cscale(CONJ ? cmulc(a[j], s) : cmul(a[j], s), scale);
     }
   } else {
     const float2* cN = bh + (long long)(N / 2) * N;
 #pragma unroll
-    for (int j = 0; j < 16; ++j) {
+    for (int j = 0; j < R; ++j) {
       const float2 s0 = __ldg(c0 + g + G * j);
       const float2 sN = __ldg(cN + g + G * j);
-      const float2 p0 = CONJ ? cmulc(a[j], s0) : cmul(a[j], s0);
-      const float2 pN = CONJ ? cmulc(b[j], sN) : cmul(b[j], sN);
+      const float2 p0 = CONJ ? cmulc(stash[j * G + g], s0) : cmul(stash[j * G + g], s0);
+      const float2 pN = CONJ ? cmulc(stash[N + j * G + g], sN) : cmul(stash[N + j * G + g], sN);
       out[j] = make_float2((p0.x - pN.y) * scale, (p0.y + pN.x) * scale);
+    }
+  }
+}
+
+// Regularised division of the column spectrum y by a cached spectrum s
+// (comp_ola_deconv_Kernel, gputools.cu:316-341):
+//   z = conj(s) y / (|s|^2 + alpha L + beta),  L(k0, k1) = lap[k1] + lap[k0],
+// scaled by `scale`, packed like column_product (u == 0: from the DC stash).
+// out may alias a.
+template <int N>
+__device__ __forceinline__ void column_divide(const float2 (&a)[FftShape<N>::R], const float2* stash,
+                                              const float2* __restrict__ bh, const float* __restrict__ lap,
+                                              int u, int g, float alpha, float beta, float scale,
+                                              float2 (&out)[FftShape<N>::R]) {
+  constexpr int G = FftShape<N>::G;
+  constexpr int R = FftShape<N>::R;
+  const float2* c0 = bh + (long long)u * N;
+  if (u != 0) {
+    const float ru = fmaf(alpha, __ldg(lap + u), beta);
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+      const float2 s = __ldg(c0 + g + G * j);
+      const float den = fmaf(s.x, s.x, s.y * s.y) + fmaf(alpha, __ldg(lap + g + G * j), ru);
+      out[j] = cscale(cmulc(a[j], s), scale / den);
+    }
+  } else {
+    const float2* cN = bh + (long long)(N / 2) * N;
+    const float r0 = fmaf(alpha, __ldg(lap), beta), rN = fmaf(alpha, __ldg(lap + N / 2), beta);
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+      const float2 s0 = __ldg(c0 + g + G * j);
+      const float2 sN = __ldg(cN + g + G * j);
+      const float lk = alpha * __ldg(lap + g + G * j);
+      const float d0 = fmaf(s0.x, s0.x, s0.y * s0.y) + (lk + r0);
+      const float dN = fmaf(sN.x, sN.x, sN.y * sN.y) + (lk + rN);
+      const float2 p0 = cscale(cmulc(stash[j * G + g], s0), scale / d0);
+      const float2 pN = cscale(cmulc(stash[N + j * G + g], sN), scale / dN);
+      out[j] = make_float2(p0.x - pN.y, p0.y + pN.x);
     }
   }
 }
@@ -343,17 +407,17 @@ __device__ __forceinline__ void column_product(const float2 (&a)[16], const floa
 template <int N, int HP>
 __device__ __forceinline__ void fwd_both_dc(float2* frame, int dcN, int rowsA, int baseB, int rowsB, int E0,
                                             int g, float2* scr, const float2* tw, unsigned gmask,
-                                            float scale, float2* a_out, float2* b_out) {
+                                            float scale, float2* a_out, float2* b_out, float2* stash) {
   constexpr int G = FftShape<N>::G;
-  float2 prod[16];
+  constexpr int R = FftShape<N>::R;
+  float2 v[R];
 #pragma unroll 1
   for (int half = 0; half < 2; ++half) {
     const int lcol = half ? dcN : 0;     // local column in the frame
     const int col = half ? N / 2 : 0;    // bin (spectrum layout)
-    float2 v[16];
     float amax = 0.f, bmax = 0.f;
 #pragma unroll
-    for (int mm = 0; mm < 16; ++mm) {
+    for (int mm = 0; mm < R; ++mm) {
       const int r = g + G * mm;
       v[mm] = make_float2(r < rowsA ? frame[r * HP + lcol].x : 0.f,
                           r < rowsB ? frame[(baseB + r) * HP + lcol].x : 0.f);
@@ -372,22 +436,28 @@ __device__ __forceinline__ void fwd_both_dc(float2* frame, int dcN, int rowsA, i
     const int e = (amax > 0.f && bmax > 0.f) ? ilogbf(amax) - ilogbf(bmax) : 0;
     const float up = ldexpf(1.f, e), down = ldexpf(0.5f, -e);  // down folds the split's 1/2
 #pragma unroll
-    for (int mm = 0; mm < 16; ++mm) v[mm].y *= up;
+    for (int mm = 0; mm < R; ++mm) v[mm].y *= up;
     fft_fwd<N>(v, g, scr, tw, gmask);
-    float2 p[16];
+    float2 p[R];
     hermitian_partner<N>(v, p, g, gmask);
 #pragma unroll
-    for (int j = 0; j < 16; ++j) {
+    for (int j = 0; j < R; ++j) {
       const float2 sa = make_float2(0.5f * (v[j].x + p[j].x), 0.5f * (v[j].y - p[j].y));
       const float2 sb = make_float2(down * (v[j].y + p[j].y), down * (p[j].x - v[j].x));
       if (a_out) a_out[(long long)col * N + g + G * j] = sa;
       if (b_out) b_out[(long long)col * N + g + G * j] = sb;
       const float2 pj = cscale(cmul(sa, sb), scale);
-      prod[j] = half ? make_float2(prod[j].x - pj.y, prod[j].y + pj.x) : pj;
+      // column 0's product waits in the stash; column N/2's joins it as i*pj
+      if (half == 0) {
+        stash[j * G + g] = pj;
+      } else {
+        const float2 z0 = stash[j * G + g];
+        v[j] = make_float2(z0.x - pj.y, z0.y + pj.x);
+      }
     }
   }
-  fft_inv<N>(prod, g, scr, tw, gmask);
-  store_column<N, HP>(frame, 0, true, dcN, 0, E0, g, prod);
+  fft_inv<N>(v, g, scr, tw, gmask);
+  store_column<N, HP>(frame, 0, true, dcN, 0, E0, g, v);
 }
 
 // One patch `k` of image `b` through the three phases, on this CTA (and its
@@ -398,6 +468,7 @@ template <int N, int OP, int CL>
 __device__ __forceinline__ void eff_patch(const Params& P, int k, long long b, float2* smem, int cta,
                                           int ncta) {
   constexpr int G = FftShape<N>::G;
+  constexpr int R = FftShape<N>::R;
   constexpr int A = opnd_a(OP);
   constexpr int HP = frame_pitch(N, CL);
   float2* tw = smem;         // N entries
@@ -444,6 +515,7 @@ __device__ __forceinline__ void eff_patch(const Params& P, int k, long long b, f
   const int rowsA = opnd_rows(P, A);
   const int baseB = even_up(rowsA);
   float2* scr = frame + frame_rows(P, OP) * HP + gid * FftShape<N>::SCR;
+  float2* stash = frame + frame_rows(P, OP) * HP + NG * FftShape<N>::SCR;  // 2N, DC unit only
 
   for (int i = tid; i < N; i += blockDim.x) tw[i] = __ldg(P.tw + i);
 
@@ -469,7 +541,7 @@ __device__ __forceinline__ void eff_patch(const Params& P, int k, long long b, f
     const int nA = (rowsA + 1) >> 1;
     const int nB = has_b(OP) ? (P.sf0 + 1) >> 1 : 0;
     for (int u = wid; u < nA + nB; u += NW) {
-      float2 v[16];
+      float2 v[R];
       int row;
       if (u < nA) {
         load_rows<N, A>(P, T, 2 * u, g, v);
@@ -492,39 +564,46 @@ __device__ __forceinline__ void eff_patch(const Params& P, int k, long long b, f
     const int col = lu;
     if constexpr (OP == OP_FWD_BOTH) {
       if (u == 0) {
-        fwd_both_dc<N, HP>(frame, dcN, rowsA, baseB, P.sf0, P.E0, g, scr, tw, gmask, scale, a_out, b_out);
+        fwd_both_dc<N, HP>(frame, dcN, rowsA, baseB, P.sf0, P.E0, g, scr, tw, gmask, scale, a_out, b_out,
+                           stash);
         continue;
       }
     }
-    float2 a[16], ab[16];
-    column_spectrum<N, HP>(frame, u, col, dcN, 0, rowsA, g, scr, tw, gmask, a, ab);
+    // column spectrum of operand A (u == 0: split into the DC stash)
+    float2 a[R];
+    load_column<N, HP>(frame, col, u == 0, dcN, 0, rowsA, g, a);
+    fft_fwd<N>(a, g, scr, tw, gmask);
+    if (u == 0) dc_split<N>(a, stash, g, gmask);
     if constexpr (OP == OP_SPEC_IMAGE || OP == OP_SPEC_PSF) {
-      store_spectrum<N>(a_out, u, g, a, ab);
+      store_spectrum<N>(a_out, u, g, a, stash);
     } else if constexpr (OP == OP_FWD_IMAGE || OP == OP_FWD_PSF) {
-      if (a_out) store_spectrum<N>(a_out, u, g, a, ab);
-      float2 pr[16];
-      column_product<N, false>(a, ab, b0, u, g, scale, pr);
-      fft_inv<N>(pr, g, scr, tw, gmask);
-      store_column<N, HP>(frame, col, u == 0, dcN, 0, P.E0, g, pr);
+      if (a_out) store_spectrum<N>(a_out, u, g, a, stash);
+      column_product<N, false>(a, stash, b0, u, g, scale, a);
+      fft_inv<N>(a, g, scr, tw, gmask);
+      store_column<N, HP>(frame, col, u == 0, dcN, 0, P.E0, g, a);
     } else if constexpr (OP == OP_FWD_BOTH) {
       // u != 0 here: a holds the image column spectrum; transform the PSF
       // column through the same code and multiply in place
-      if (a_out) store_spectrum<N>(a_out, u, g, a, ab);
-      float2 s[16];
+      if (a_out) store_spectrum<N>(a_out, u, g, a, stash);
+      float2 s[R];
       load_column<N, HP>(frame, col, false, dcN, baseB, P.sf0, g, s);
       fft_fwd<N>(s, g, scr, tw, gmask);
-      if (b_out) store_spectrum<N>(b_out, u, g, s, s);
+      if (b_out) store_spectrum<N>(b_out, u, g, s, stash);
 #pragma unroll
-      for (int j = 0; j < 16; ++j) a[j] = cscale(cmul(a[j], s[j]), scale);
+      for (int j = 0; j < R; ++j) a[j] = cscale(cmul(a[j], s[j]), scale);
       fft_inv<N>(a, g, scr, tw, gmask);
       store_column<N, HP>(frame, col, false, dcN, 0, P.E0, g, a);
     } else {
-      // adjoints: output 0 = image (conj F-hat, rows sw0), 1 = PSF (conj X-hat, rows sf0)
+      // adjoints: output 0 = image (conj F-hat, rows sw0), 1 = PSF (conj X-hat, rows sf0);
+      // deconv: the same outputs from the regularised division
 #pragma unroll 1
       for (int o = 0; o < 2; ++o) {
         if (o == 0 ? !P.out0 : !P.out1) continue;
-        float2 pr[16];
-        column_product<N, true>(a, ab, o == 0 ? b0 : b1, u, g, scale, pr);
+        float2 pr[R];
+        if constexpr (OP == OP_DECONV)
+          column_divide<N>(a, stash, o == 0 ? b0 : b1, P.lap, u, g, P.alpha, P.beta, scale, pr);
+        else
+          column_product<N, true>(a, stash, o == 0 ? b0 : b1, u, g, scale, pr);
         fft_inv<N>(pr, g, scr, tw, gmask);
         const int base = (o == 1 && P.out0) ? even_up(P.sw0) : 0;
         store_column<N, HP>(frame, col, u == 0, dcN, base, o == 0 ? P.sw0 : P.sf0, g, pr);
@@ -545,12 +624,12 @@ __device__ __forceinline__ void eff_patch(const Params& P, int k, long long b, f
     const int i0 = T.m * P.hop0 - P.off0, j0 = T.n * P.hop1 - P.off1;
     const int nu = (P.E0 + 1) >> 1;
     for (int u = wid; u < nu; u += NW) {
-      float2 v[16];
+      float2 v[R];
       c2r_unit<N, CL>(F, 2 * u, v, scr, tw, g, gmask);
       const int ia = i0 + 2 * u;
       const bool rb = 2 * u + 1 < P.E0;
 #pragma unroll
-      for (int mm = 0; mm < 16; ++mm) {
+      for (int mm = 0; mm < R; ++mm) {
         const int c = g + G * mm, j = j0 + c;
         if (c < P.E1 && j >= 0 && j < P.sy1) {
           if (ia >= 0 && ia < P.sy0) atomicAdd(out + (long long)ia * P.sy1 + j, v[mm].x);
@@ -558,30 +637,35 @@ __device__ __forceinline__ void eff_patch(const Params& P, int k, long long b, f
         }
       }
     }
-  } else if constexpr (OP == OP_ADJ) {
+  } else if constexpr (OP == OP_ADJ || OP == OP_DECONV) {
     const int n0 = P.out0 ? (P.sw0 + 1) >> 1 : 0;
     const int n1 = P.out1 ? (P.sf0 + 1) >> 1 : 0;
     const int base1 = P.out0 ? even_up(P.sw0) : 0;
     for (int u = wid; u < n0 + n1; u += NW) {
       const bool img = u < n0;
       const int r = img ? 2 * u : 2 * (u - n0);
-      float2 v[16];
+      float2 v[R];
       c2r_unit<N, CL>(F, img ? r : base1 + r, v, scr, tw, g, gmask);
       if (img) {
-        // image gradient: window, overlap-add into gx
+        // image gradient: window, overlap-add into gx (deconv: overlap-add
+        // of the sw crop without a window, olaGPU.py:602-607)
         float* out = P.out0 + b * P.out0_bs;
         const int i = T.m * P.hop0 + r;
         const bool rb = r + 1 < P.sw0;
         const float2 wa = __ldg(P.win0 + T.m * P.sw0 + r);
         const float2 wb = rb ? __ldg(P.win0 + T.m * P.sw0 + r + 1) : make_float2(0.f, 0.f);
 #pragma unroll
-        for (int mm = 0; mm < 16; ++mm) {
+        for (int mm = 0; mm < R; ++mm) {
           const int c = g + G * mm, j = T.n * P.hop1 + c;
           if (c < P.sw1 && j < P.sx1) {
-            const float2 wc = __ldg(P.win1 + T.n * P.sw1 + c);
-            if (i < P.sx0) atomicAdd(out + (long long)i * P.sx1 + j, v[mm].x * window_weight(wa, wc));
-            if (rb && i + 1 < P.sx0)
-              atomicAdd(out + (long long)(i + 1) * P.sx1 + j, v[mm].y * window_weight(wb, wc));
+            float w0 = 1.f, w1 = 1.f;
+            if constexpr (OP == OP_ADJ) {
+              const float2 wc = __ldg(P.win1 + T.n * P.sw1 + c);
+              w0 = window_weight(wa, wc);
+              w1 = window_weight(wb, wc);
+            }
+            if (i < P.sx0) atomicAdd(out + (long long)i * P.sx1 + j, v[mm].x * w0);
+            if (rb && i + 1 < P.sx0) atomicAdd(out + (long long)(i + 1) * P.sx1 + j, v[mm].y * w1);
           }
         }
       } else {
@@ -589,7 +673,7 @@ __device__ __forceinline__ void eff_patch(const Params& P, int k, long long b, f
         float* out = P.out1 + b * P.out1_bs + (long long)T.k * P.sf0 * P.sf1;
         const bool rb = r + 1 < P.sf0;
 #pragma unroll
-        for (int mm = 0; mm < 16; ++mm) {
+        for (int mm = 0; mm < R; ++mm) {
           const int c = g + G * mm;
           if (c < P.sf1) {
             out[r * P.sf1 + c] = v[mm].x;

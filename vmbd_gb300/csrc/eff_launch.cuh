@@ -6,12 +6,12 @@
 namespace eff {
 
 // Shared-memory bytes of one CTA: twiddles + frame (its share of the columns)
-// + per-group exchange scratch.
+// + per-group exchange scratch + the DC unit's stash (2N).
 inline size_t smem_bytes(int N, int op, const Params& P, int threads, int CL) {
-  const int G = N / 16;
-  const int scr = 16 * (G + 1) + 8;
+  const int R = lane_values(N), G = N / R;
+  const int scr = R * (G + 1) + 8;
   return sizeof(float2) * ((size_t)N + (size_t)frame_rows(P, op) * frame_pitch(N, CL) +
-                           (size_t)(threads / G) * scr);
+                           (size_t)(threads / G) * scr + 2 * (size_t)N);
 }
 
 template <int N, int OP, int CL>
@@ -56,6 +56,7 @@ cudaError_t launch_ncl(int op, const Params& P, int K, int batch, int threads, s
     case OP_FWD_PSF: return launch_one<N, OP_FWD_PSF, CL>(P, K, batch, threads, smem, st);
     case OP_FWD_BOTH: return launch_one<N, OP_FWD_BOTH, CL>(P, K, batch, threads, smem, st);
     case OP_ADJ: return launch_one<N, OP_ADJ, CL>(P, K, batch, threads, smem, st);
+    case OP_DECONV: return launch_one<N, OP_DECONV, CL>(P, K, batch, threads, smem, st);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -69,6 +70,7 @@ cudaError_t launch_n(int op, int CL, const Params& P, int K, int batch, int thre
 
 cudaError_t launch_n64(int op, int CL, const Params& P, int K, int batch, int threads, size_t smem, cudaStream_t st);
 cudaError_t launch_n128(int op, int CL, const Params& P, int K, int batch, int threads, size_t smem, cudaStream_t st);
+cudaError_t launch_n192(int op, int CL, const Params& P, int K, int batch, int threads, size_t smem, cudaStream_t st);
 cudaError_t launch_n256(int op, int CL, const Params& P, int K, int batch, int threads, size_t smem, cudaStream_t st);
 
 }  // namespace eff

@@ -30,7 +30,7 @@ class EffPlan:
     """Plan for ``y = EFF(x, f)`` on one geometry (OlaGPU.__init__,
     olaGPU.py:95-168, without the cached spectrum)."""
 
-    def __init__(self, winaux: Winaux, sf, mode: str = "valid", sfft: int = 0, device=None):
+    def __init__(self, winaux: Winaux, sf, mode: str = "valid", sfft: int = 0, device=None, threads: int = 0):
         if mode not in _lib.MODES:
             raise NotImplementedError("Not a valid mode!")
         self.lib = _lib.load()
@@ -48,6 +48,7 @@ class EffPlan:
         g.sw[:] = winaux.sw
         g.hop[:] = winaux.nhop
         g.sfft = int(sfft)
+        g.threads = int(threads)
         g.mode = _lib.MODES[mode]
         self._w0 = np.ascontiguousarray(winaux.win0, dtype=np.float32)
         self._w1 = np.ascontiguousarray(winaux.win1, dtype=np.float32)
@@ -242,6 +243,32 @@ class EffPlan:
                                                  _ptr(xhat if want_psf else None), _ptr(gx), _ptr(gf),
                                                  _ptr(loss), mode, b or 1, _stream(self.device)))
         return loss, gx, gf
+
+    def deconv_xdirect(self, y, fhat=None, xhat=None, alpha: float = 0.0, beta: float = 0.01, u=None, fz=None):
+        """OlaGPU.deconv(y, mode='xdirect'), olaGPU.py:550-609: per-patch
+        division ``conj(S) Y / (|S|^2 + alpha L + beta)`` in this plan's
+        N x N frame.  ``fhat`` (F object) gives the image estimate ``u``
+        [..., sx]; ``xhat`` (X object) the PSF estimate ``fz`` [..., K, sf].
+        Returns ``(u, fz)``; an output that is not asked for is None."""
+        if self.mode not in ("valid", "same"):
+            raise NotImplementedError("Not a valid mode!")
+        if fhat is None and xhat is None:
+            raise ValueError("deconv_xdirect needs fhat (image estimate) and/or xhat (PSF estimate)")
+        y, b = self._check(y, self.sy, "y")
+        lead = (b,) if b else ()
+        if fhat is not None:
+            self._check_spec(fhat, b, "fhat")
+            if u is None:
+                u = torch.empty(lead + self.sx, dtype=torch.float32, device=self.device)
+        if xhat is not None:
+            self._check_spec(xhat, b, "xhat")
+            if fz is None:
+                fz = torch.empty(lead + (self.K,) + self.sf, dtype=torch.float32, device=self.device)
+        _lib.check(self.lib.eff_deconv_xdirect(self._h, _ptr(y), _ptr(fhat), _ptr(xhat),
+                                               _ptr(u if fhat is not None else None),
+                                               _ptr(fz if xhat is not None else None), float(alpha),
+                                               float(beta), b or 1, _stream(self.device)))
+        return (u if fhat is not None else None), (fz if xhat is not None else None)
 
 
 def project_psf(f: torch.Tensor, mode: str = "simplex") -> torch.Tensor:

@@ -123,11 +123,78 @@ class OlaGPU:
                                                     adjoint=self.adjoint)
         return float(loss), g
 
-    def deconv(self, y, z0=None, mode="lbfgsb", maxfun=100, alpha=0.0, beta=0.01, verbose=-1, m=5):
-        """OlaGPU.deconv (olaGPU.py:315-412) for mode 'lbfgsb': the PSFs (X
-        object) or the image (F object) minimising 0.5||y - Z u||^2 +
-        0.5 beta ||u||^2, u >= 0.  Returns (u, f(u), info)."""
-        if mode != "lbfgsb":
+    def deconv(self, y, z0=None, mode="lbfgsb", maxfun=100, alpha=0.0, beta=0.01, verbose=-1, m=5,
+               edgetapering=1, factor=3):
+        """OlaGPU.deconv (olaGPU.py:312-733) for modes
+
+        * 'lbfgsb' (:381-412): the PSFs (X object) or the image (F object)
+          minimising 0.5||y - Z u||^2 + 0.5 beta ||u||^2, u >= 0; returns
+          (u, f(u), info);
+        * 'xdirect' (:550-609): per-patch regularised division in Fourier
+          space, conj(S) Y / (|S|^2 + alpha L + beta); returns the image
+          estimate (F object) or the PSF estimates (X object);
+        * 'direct' (:515-548, F object): 'xdirect' corrected by the
+          'xdirect' of a constant image, border cropped and replicate-padded.
+
+        The division depends on the FFT frame: it runs in the reference's
+        frame, the power of two >= sw + sf - 1 (one per dim; a non-square one
+        raises NotImplementedError).  ``edgetapering`` only changes 'direct'
+        (in 'xdirect' the reference tapers a copy that its chop never reads).
+        """
+        t, host = _to_device(y, self.device)
+        if tuple(t.shape) != tuple(self.sy):
+            raise IOError("Sizes incompatible. Expected blurred image!")
+        if mode == "lbfgsb":
+            from .optim import deconv_lbfgsb
+            return deconv_lbfgsb(self, t, z0=z0, maxfun=maxfun, alpha=alpha, beta=beta, verbose=verbose, m=m)
+        if mode == "xdirect":
+            out = self._xdirect(t, alpha, beta)
+        elif mode == "direct":
+            if self.__id__ != "F":
+                raise NotImplementedError("'direct' estimates the image: use an F object")
+            out = self._direct(t, alpha, beta, edgetapering, factor)
+        else:
             raise NotImplementedError("Not a valid mode!")
-        from .optim import deconv_lbfgsb
-        return deconv_lbfgsb(self, y, z0=z0, maxfun=maxfun, alpha=alpha, beta=beta, verbose=verbose, m=m)
+        return out.cpu().numpy() if host else out
+
+    def _deconv_plan(self):
+        """(plan, cached spectrum) in the reference's FFT frame
+        (olaGPU.py:139-141): this object's own plan when its frame is that
+        one, else a second plan with the spectrum recomputed there."""
+        if self.mode not in ("valid", "same"):
+            raise NotImplementedError("Not a valid mode!")
+        E = [self.winaux.sw[d] + self.sf[d] - 1 for d in range(2)]
+        ref = [1 << int(np.ceil(np.log2(e))) for e in E]
+        if ref[0] != ref[1] or ref[0] not in (64, 128, 256):
+            raise NotImplementedError(f"deconv: the reference frame {ref[0]}x{ref[1]} is not one of the "
+                                      "square frames 64, 128, 256")
+        if ref[0] == self.plan.N:
+            return self.plan, self.fft_gpu
+        if getattr(self, "_dplan", None) is None:
+            plan = EffPlan(self.winaux, self.sf, self.mode, sfft=ref[0], device=self.device)
+            spec = plan.psf_spectrum(self.f) if self.__id__ == "F" else plan.image_spectrum(self.x)
+            self._dplan = (plan, spec)
+        return self._dplan
+
+    def _xdirect(self, y, alpha, beta):
+        plan, spec = self._deconv_plan()
+        if self.__id__ == "F":
+            return plan.deconv_xdirect(y, fhat=spec, alpha=alpha, beta=beta)[0]
+        return plan.deconv_xdirect(y, xhat=spec, alpha=alpha, beta=beta)[1]
+
+    def _direct(self, y, alpha, beta, edgetapering, factor):
+        from .gputools import edgetaper_gpu, impad_gpu
+        sf = np.asarray(self.sf, dtype=np.int64)
+        u = self._xdirect(y, alpha, beta).clamp_min_(0.0)
+        const = torch.ones(tuple(self.sy), dtype=torch.float32, device=self.device)
+        if edgetapering == 1:
+            edgetaper_gpu(const, 2 * sf)
+        c = self._xdirect(const, alpha, beta)
+        edgetaper_gpu(c, 2 * sf)
+        c.clamp_(0.01, 10.0)
+        u = u / c
+        sz = np.asarray(u.shape, dtype=np.int64)
+        csz = sz - factor * sf - 1
+        off = np.floor((factor * sf - 1) / 2.0).astype(np.int64)
+        u = u[off[0]:off[0] + csz[0], off[1]:off[1] + csz[1]].contiguous()
+        return impad_gpu(u, sz - csz)

@@ -108,6 +108,31 @@ class UnfusedEff:
         zf = torch.fft.ifft2(yh * xhat.conj()).real[:, :self.sf[0], :self.sf[1]].contiguous()
         return gx, zf
 
+    def xdirect(self, y, fhat=None, xhat=None, alpha=0.0, beta=0.01):
+        """OlaGPU.deconv 'xdirect' (olaGPU.py:550-609) stage by stage: chop of
+        y at frame offset ``off`` times the window at the frame origin -> FFT
+        -> regularised division (one elementwise pass per stage) -> inverse
+        FFT -> crop to sw + overlap-add (image) / crop to sf (PSFs)."""
+        N = self.N
+        o = self.off
+        emb = F.pad(y, (o[1], 0, o[0], 0))
+        u = self._chop(emb, self.ii, self.jj, self.sw) * self.ws
+        u = F.pad(u, (0, N - self.sw[1], 0, N - self.sw[0]))
+        yh = torch.fft.fft2(u.to(torch.complex64))
+        reg = beta
+        if alpha > 0:
+            k = torch.arange(N, device=y.device, dtype=torch.float64)
+            lap = (4.0 * torch.sin(torch.pi * k / N) ** 2).to(torch.float32)
+            reg = alpha * (lap[:, None] + lap[None, :]) + beta
+        img = psf = None
+        if fhat is not None:
+            z = torch.fft.ifft2(fhat.conj() * yh / (fhat.abs() ** 2 + reg)).real[:, :self.sw[0], :self.sw[1]]
+            img = self._ola(z.contiguous(), self.sw, self.sx)
+        if xhat is not None:
+            z = torch.fft.ifft2(xhat.conj() * yh / (xhat.abs() ** 2 + reg)).real
+            psf = z[:, :self.sf[0], :self.sf[1]].contiguous()
+        return img, psf
+
     # -- pieces used by the unfused MFBD comparator ---------------------------
     def forward_from_spectra(self, xh, fh):
         ys = torch.fft.ifft2(fh * xh)
