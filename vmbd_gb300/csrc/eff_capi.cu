@@ -133,9 +133,10 @@ int check_plan(const EffPlan* p, int batch) {
   return EFF_OK;
 }
 
+// zeroed: gx and loss were already zeroed on the stream (by the fused forward).
 int adjoint_impl(const EffPlan* plan, const float* y, const float* y_obs, const void* fhat,
                  const void* xhat, float* gx, float* gf, double* loss, int adj_mode, int batch,
-                 void* stream, const float* mask = nullptr) {
+                 void* stream, const float* mask = nullptr, bool zeroed = false) {
   if (int s = check_plan(plan, batch)) return s;
   if (!y || (!gx && !gf)) return fail(EFF_ERR_INVALID, "null argument");
   if (gx && !fhat) return fail(EFF_ERR_INVALID, "image adjoint needs the PSF spectrum");
@@ -163,11 +164,11 @@ int adjoint_impl(const EffPlan* plan, const float* y, const float* y_obs, const 
     P.hi1 = plan->off[1] + plan->g.sw[1] < plan->E[1] ? plan->off[1] + plan->g.sw[1] : plan->E[1];
   }
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  if (gx) {
+  if (gx && !zeroed) {
     cudaError_t e = cudaMemsetAsync(gx, 0, sizeof(float) * P.x_bs * batch, st);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
   }
-  if (loss) {
+  if (loss && !zeroed) {
     cudaError_t e = cudaMemsetAsync(loss, 0, sizeof(double) * batch, st);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
   }
@@ -212,12 +213,17 @@ int loss_grad_impl(const EffPlan* plan, const float* x, const float* f, const fl
   P.b_out = gx ? fhat : nullptr;
   P.pf = reinterpret_cast<const char*>(y_obs);
   P.pf_bytes = (long long)sizeof(float) * P.y_bs;
+  // the forward also zeroes the adjoint's accumulators (no memset nodes)
+  P.zero_f = gx;
+  P.zero_nf = gx ? P.x_bs * batch : 0;
+  P.zero_d = loss;
+  P.zero_nd = loss ? batch : 0;
   cudaError_t e = cudaMemsetAsync(y, 0, sizeof(float) * P.y_bs * batch, static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
   int s = run(plan, eff::OP_FWD_BOTH, P, batch, stream);
   if (s != EFF_OK) return s;
   return adjoint_impl(plan, y, y_obs, gx ? fhat : nullptr, gf ? xhat : nullptr, gx, gf, loss,
-                      EFF_ADJ_EXACT, batch, stream);
+                      EFF_ADJ_EXACT, batch, stream, nullptr, true);
 }
 
 }  // namespace

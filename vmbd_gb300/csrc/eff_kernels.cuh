@@ -70,6 +70,10 @@ struct Params {
   long long pf_bytes;
   const float* lap;        // deconv: 4 sin^2(pi k / N), k < N (spectrum of the difference filters)
   float alpha, beta;       // deconv: regularisation weights
+  float* zero_f;           // eff_kernel: zero [zero_f, zero_f + zero_nf) (the next kernel's
+  long long zero_nf;       //   accumulator), spread over the grid
+  double* zero_d;          // eff_kernel: zero [zero_d, zero_d + zero_nd)
+  int zero_nd;
 };
 
 // TMA bulk prefetch of a contiguous range into L2 (16-byte aligned start and
@@ -706,10 +710,29 @@ __device__ __forceinline__ void eff_patch(const Params& P, int k, long long b, f
   if constexpr (CL > 1) phase_sync();
 }
 
+// Zero the accumulators of the kernel that follows in the same stream (a
+// grid-stride share per CTA), so that it needs no memset of its own.
+__device__ __forceinline__ void zero_next(const Params& P) {
+  const long long cta = (long long)blockIdx.y * gridDim.x + blockIdx.x;
+  const long long ncta = (long long)gridDim.x * gridDim.y;
+  if (P.zero_f) {
+    const long long n = P.zero_nf;
+    const bool vec = (reinterpret_cast<unsigned long long>(P.zero_f) & 15ull) == 0;
+    const long long n4 = vec ? n / 4 : 0;
+    float4* p4 = reinterpret_cast<float4*>(P.zero_f);
+    for (long long i = cta * blockDim.x + threadIdx.x; i < n4; i += ncta * blockDim.x)
+      p4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (long long i = 4 * n4 + cta * blockDim.x + threadIdx.x; i < n; i += ncta * blockDim.x) P.zero_f[i] = 0.f;
+  }
+  if (P.zero_d && cta == 0)
+    for (int i = threadIdx.x; i < P.zero_nd; i += blockDim.x) P.zero_d[i] = 0.0;
+}
+
 // One patch per CTA (CL = 1) or per 2-CTA cluster, images along blockIdx.y.
 template <int N, int OP, int CL>
 __global__ void __launch_bounds__(max_threads(N)) eff_kernel(Params P) {
   extern __shared__ __align__(16) float2 smem[];
+  if constexpr (OP == OP_FWD_BOTH) zero_next(P);
   eff_patch<N, OP, CL>(P, blockIdx.x / CL, blockIdx.y, smem, blockIdx.x, gridDim.x);
 }
 
