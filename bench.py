@@ -325,6 +325,23 @@ def profile_run(args, dev):
         torch.cuda.synchronize(dev)
         print(json.dumps({"profile": "mfbd", "frames": args.warmup + args.steps}))
         return
+    if args.workload == "deconv":
+        # Fourier-division deconvolution on the 512^2 / 8x8 / 96^2 / 31^2 geometry:
+        # image and PSF estimates from one call per step
+        w = WORKLOADS["cfg2"]
+        wa, x_np, f_np = make_inputs(w, seed=3)
+        plan = EffPlan(wa, w["sf"], "valid", device=dev)
+        x = torch.from_numpy(x_np).to(dev)
+        f = torch.from_numpy(f_np).to(dev)
+        fh, xh = plan.psf_spectrum(f), plan.image_spectrum(x)
+        y = plan.forward_image(x, fh)
+        flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+        for _ in range(args.warmup + args.steps):
+            flush.fill_(1.0)
+            plan.deconv_xdirect(y, fhat=fh, xhat=xh, alpha=1e-2, beta=1e-2)
+        torch.cuda.synchronize(dev)
+        print(json.dumps({"profile": "deconv", "steps": args.warmup + args.steps}))
+        return
     if args.workload == "cfg4":
         from vmbd_gb300.eff import EffBatch
         plans, counts, xs, fs, yo = cfg4_data(dev)
@@ -580,7 +597,7 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=list(WORKLOADS) + ["mfbd", "cfg4"], default="cfg2")
+    ap.add_argument("--workload", choices=list(WORKLOADS) + ["mfbd", "cfg4", "deconv"], default="cfg2")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile", action="store_true",
                     help="short eager run of the step only (for an ncu launch list / capture)")
@@ -594,6 +611,8 @@ def main():
         return main_mfbd(args, world, rank, local)
     if args.workload == "cfg4" and not args.profile:
         return main_cfg4(args, world, rank, local)
+    if args.workload == "deconv" and not args.profile:
+        ap.error("--workload deconv is a --profile mode; its timing is part of the default bench line")
     if args.profile:
         import torch
         torch.cuda.set_device(local)
