@@ -536,6 +536,20 @@ __device__ __forceinline__ void eff_patch(const Params& P, int k, long long b, f
         l2_prefetch_bulk(a, (unsigned)n);
     }
   }
+  // Kernels that multiply by a cached spectrum in the column pass: pull the
+  // columns this CTA owns into L2 now, so that a cold spectrum arrives while
+  // the row pass runs (TMA bulk prefetch; a hint, the loads stay as they are).
+  if constexpr (OP == OP_FWD_IMAGE || OP == OP_FWD_PSF || OP == OP_ADJ || OP == OP_DECONV) {
+    if (tid < 2) {
+      const float2* sp = tid == 0 ? b0 : b1;
+      if (sp && (reinterpret_cast<unsigned long long>(sp) & 15ull) == 0) {
+        const int c0 = CL == 1 ? 0 : F.rank * (N / 4);
+        const int nc = CL == 1 ? N / 2 + 1 : N / 4;
+        l2_prefetch_bulk(sp + (long long)c0 * N, (unsigned)(nc * N * sizeof(float2)));
+        if (CL > 1 && F.rank == 0) l2_prefetch_bulk(sp + (long long)(N / 2) * N, (unsigned)(N * sizeof(float2)));
+      }
+    }
+  }
   // The peer must not write into this CTA's frame before it is running (and,
   // in a persistent loop, before this CTA has finished the previous patch).
   phase_sync();

@@ -194,14 +194,15 @@ class EffPlan:
         return loss, gx, gf
 
     def adjoint_residual(self, y, y_obs, fhat=None, xhat=None, want_image=True, want_psf=True,
-                         loss=None, gx=None, gf=None, adjoint="exact"):
+                         loss=None, gx=None, gf=None, adjoint="exact", want_loss=True):
         """``adjoint(y - y_obs)`` without forming the residual; also returns
-        ``0.5*||y - y_obs||^2`` (float64).  Returns ``(loss, gx, gf)``."""
+        ``0.5*||y - y_obs||^2`` (float64; None when ``want_loss`` is False,
+        which skips its reduction).  Returns ``(loss, gx, gf)``."""
         return self.adjoint(y, fhat, xhat, want_image, want_psf, adjoint, gx, gf, y_obs=y_obs,
-                            loss=loss)
+                            loss=loss, want_loss=want_loss)
 
     def adjoint(self, y, fhat=None, xhat=None, want_image=True, want_psf=True,
-                adjoint="exact", gx=None, gf=None, y_obs=None, loss=None):
+                adjoint="exact", gx=None, gf=None, y_obs=None, loss=None, want_loss=True):
         """F.cnvtp(y) and/or X.cnvtp(y) from one transform of y.
 
         Returns ``(gx, gf)``; an output that is not wanted is None.
@@ -236,7 +237,9 @@ class EffPlan:
                                             b or 1, _stream(self.device)))
             return gx, gf
         y_obs, _ = self._check(y_obs, self.sy, "y_obs")
-        if loss is None:
+        if not want_loss:
+            loss = None
+        elif loss is None:
             loss = torch.empty(lead, dtype=torch.float64, device=self.device)
         _lib.check(self.lib.eff_adjoint_residual(self._h, _ptr(y), _ptr(y_obs),
                                                  _ptr(fhat if want_image else None),

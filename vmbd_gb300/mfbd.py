@@ -71,7 +71,6 @@ class OnlineMFBD:
         self.num = z(self.sx)
         self.den = z(self.sx)
         self.dots = z(3, torch.float64)
-        self.loss = z(1, torch.float64)
         self.state = torch.ones(1, dtype=torch.float32, device=dev)
         self.xmax = z(1, torch.int32)
         self.nummax = z(1, torch.int32)
@@ -101,8 +100,9 @@ class OnlineMFBD:
         P.image_spectrum(self.x, out=self.xhat)
         for k in range(self.n_pg):
             P.forward_psf(self.f, self.xhat, out=self.ypred)
+            # the BB / exact-line-search steps need no objective value: no loss reduction
             P.adjoint_residual(self.ypred, self.y, xhat=self.xhat, want_image=False, gf=self.g,
-                               loss=self.loss, adjoint=self.adjoint)
+                               want_loss=False, adjoint=self.adjoint)
             if k == 0:
                 P.forward_psf(self.g, self.xhat, out=self.yg)
                 self._check(L.eff_dots3(_ptr(self.g), None, K * n, _ptr(self.yg), None, ny,
