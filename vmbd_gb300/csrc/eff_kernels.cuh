@@ -87,7 +87,7 @@ __device__ __forceinline__ void l2_prefetch_bulk(const void* p, unsigned bytes) 
 __host__ __device__ constexpr int frame_pitch(int N, int CL = 1) { return CL == 1 ? N / 2 + 1 : N / 4 + 1; }
 __host__ __device__ constexpr int even_up(int v) { return (v + 1) & ~1; }
 // Threads per CTA the kernel is compiled for (the host may launch fewer).
-__host__ __device__ constexpr int max_threads(int N) { return N % 3 == 0 ? 384 : 512; }
+__host__ __device__ constexpr int max_threads(int N) { return N % 3 == 0 ? 384 : (N == 256 ? 576 : 512); }
 
 // Operand A / B of each op, their row counts and frame bases.
 __host__ __device__ constexpr int opnd_a(int op) {

@@ -38,7 +38,7 @@ class OnlineMFBD:
     NUM_FLOOR = 1e-6
 
     def __init__(self, sy, sf, csf, overlap=0.5, n_pg=10, n_mu=5, tol=1e-10, taper=True,
-                 device=None, sw=None, nhop=None, adjoint="exact"):
+                 device=None, sw=None, nhop=None, adjoint="exact", sfft=0, threads=0):
         self.sy = (int(sy[0]), int(sy[1]))
         self.sf = (int(sf[0]), int(sf[1]))
         self.sx = tuple(self.sy[d] + self.sf[d] - 1 for d in range(2))
@@ -46,7 +46,8 @@ class OnlineMFBD:
         if self.device.index is None:
             self.device = torch.device("cuda", torch.cuda.current_device())
         self.winaux = win2winaux(self.sx, csf, overlap, sw=sw, nhop=nhop)
-        self.plan = EffPlan(self.winaux, self.sf, "valid", device=self.device)
+        # sfft / threads: FFT frame and CTA size of the plan (0: automatic)
+        self.plan = EffPlan(self.winaux, self.sf, "valid", device=self.device, sfft=sfft, threads=threads)
         self.n_pg, self.n_mu, self.tol = int(n_pg), int(n_mu), float(tol)
         self.adjoint = adjoint
         self.lib = _lib.load()
