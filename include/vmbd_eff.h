@@ -45,6 +45,11 @@ extern "C" {
 #define EFF_MODE_SAME 1
 #define EFF_MODE_FULL 2
 
+#define EFF_OUT_ZEROED 1 /* flags: the call's accumulated output is already zero (no memset) */
+
+#define EFF_OPERAND_IMAGE 0 /* eff_forward_ex: u is the image, spec the PSF spectrum */
+#define EFF_OPERAND_PSF 1   /* eff_forward_ex: u is the PSF stack, spec the image spectrum */
+
 #define EFF_ADJ_EXACT 0     /* exact transpose of the forward operator */
 #define EFF_ADJ_REFERENCE 1 /* OlaGPU.cnvtp's truncated chop (olaGPU.py:276-286) */
 
@@ -182,6 +187,25 @@ int eff_deconv_xdirect(const EffPlan* plan, const float* y, const void* fhat, co
 int eff_adjoint_masked(const EffPlan* plan, const float* y, const float* mask, const void* fhat,
                        const void* xhat, float* gx, float* gf, int adj_mode, int batch, void* stream);
 
+/* Chained calls without memsets.  Loops that run many forward / adjoint
+ * pairs in one graph (the MFBD frame) spend ~1 us per memset node; these
+ * let each accumulated output be zeroed as a side job of an earlier kernel
+ * that does not touch it, and its own call skip the memset.
+ * eff_forward_ex: eff_forward_image (operand EFF_OPERAND_IMAGE, spec =
+ *   fhat) or eff_forward_psf (EFF_OPERAND_PSF, spec = xhat); flags
+ *   EFF_OUT_ZEROED: y is already zero; zero_f[0, zero_nf) (float) and
+ *   zero_d[0, zero_nd) (double), nullable, are cleared by the kernel for a
+ *   later call and must not overlap anything this call reads or writes.
+ * eff_adjoint_ex: eff_adjoint / eff_adjoint_residual (y_obs) /
+ *   eff_adjoint_masked (mask) in one; flags EFF_OUT_ZEROED: gx and loss are
+ *   already zero. */
+int eff_forward_ex(const EffPlan* plan, int operand, const float* u, const void* spec, float* y, void* spec_out,
+                   int flags, float* zero_f, long long zero_nf, double* zero_d, int zero_nd, int batch,
+                   void* stream);
+int eff_adjoint_ex(const EffPlan* plan, const float* y, const float* y_obs, const float* mask, const void* fhat,
+                   const void* xhat, float* gx, float* gf, double* loss, int adj_mode, int flags, int batch,
+                   void* stream);
+
 /* Online MFBD helpers (vmbd_chimney.py:110-182 with projected-gradient PSF
  * steps, optGPU.py:134-358):
  * eff_dots3: out[0] = sum u^2 (na terms), out[2] = sum v^2 (nb terms),
@@ -200,15 +224,18 @@ int eff_adjoint_masked(const EffPlan* plan, const float* y, const float* mask, c
  *   Where no data reaches a pixel num and den are 0 in exact arithmetic (the
  *   factor is tol) but FP32 transform noise well above tol = 1e-10; the
  *   floor (1e-6 in vmbd_gb300.mfbd) restores the exact-arithmetic factor.
- *   xmax_bits is a device scratch word. */
+ *   xmax_bits is a device scratch word.
+ * flags EFF_OUT_ZEROED: out (eff_dots3) / xmax_bits (eff_mu_update) is
+ * already zero; zero_f[0, zero_n) (nullable) is cleared as a side job, as in
+ * eff_forward_ex. */
 int eff_dots3(const float* a, const float* ap, long long na, const float* b, const float* bp, long long nb,
-              double* out, void* stream);
+              double* out, int flags, void* stream);
 int eff_pg_step(float* f, const float* g, float* f_prev, float* g_prev, int K, int n, const double* dots,
-                int mode, float* state, void* stream);
+                int mode, float* state, float* zero_f, long long zero_n, void* stream);
 int eff_max_nonneg(const float* a, long long n, unsigned* out_bits, void* stream);
 int eff_mu_update(float* x, const float* num, const float* den, float tol, int rows, int cols, int border0,
-                  int border1, const unsigned* num_max_bits, float floor_rel, unsigned* xmax_bits,
-                  void* stream);
+                  int border1, const unsigned* num_max_bits, float floor_rel, unsigned* xmax_bits, int flags,
+                  float* zero_f, long long zero_n, void* stream);
 
 /* Uneven batches in one persistent launch (BASELINE's batched workload):
  * images of up to 8 geometries (one plan each, counts[c] images of plan c,

@@ -50,8 +50,10 @@ def test_pg_step_and_dots(cuda):
         state = torch.ones(1, device=cuda)
         dd = torch.from_numpy(ref).to(cuda)
         f2, g2, fp2, gp2 = t(f), t(g), t(fp), t(gp)
+        side = torch.ones(70001, device=cuda)  # cleared as the step's side job
         _lib.check(lib.eff_pg_step(_ptr(f2), _ptr(g2), _ptr(fp2), _ptr(gp2), K, n, _ptr(dd), mode,
-                                   _ptr(state), None))
+                                   _ptr(state), _ptr(side), side.numel(), None))
+        assert not side.any()
         s = mfbd64.step_size(ref, mode, 1.0)
         want = eff64.simplex_project(f32 - s * g32)
         assert abs(float(state) - s) < 1e-6 * s

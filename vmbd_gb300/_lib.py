@@ -18,6 +18,9 @@ EFF_ERR_CUDA = 3
 MODES = {"valid": 0, "same": 1, "full": 2}
 ADJ_EXACT = 0
 ADJ_REFERENCE = 1
+OUT_ZEROED = 1
+OPERAND_IMAGE = 0
+OPERAND_PSF = 1
 PROJ_CLIP_NORMALIZE = 0
 PROJ_SIMPLEX = 1
 
@@ -30,7 +33,8 @@ EXPORTS = (
     "eff_static_scratch_bytes", "eff_loss_grad_static", "eff_edgetaper",
     "eff_adjoint_masked", "eff_dots3", "eff_pg_step", "eff_mu_update", "eff_max_nonneg",
     "eff_set_cluster_mode", "eff_batch_create", "eff_batch_destroy", "eff_batch_items",
-    "eff_batch_forward_both", "eff_batch_adjoint_residual", "eff_deconv_xdirect",
+    "eff_batch_forward_both", "eff_batch_adjoint_residual", "eff_deconv_xdirect", "eff_forward_ex",
+    "eff_adjoint_ex",
 )
 
 
@@ -84,8 +88,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "eff_static_scratch_bytes": ([], ctypes.c_size_t),
         "eff_edgetaper": ([fp, ip, ip, fp, ip, fp, ip, ip, vp], ip),
         "eff_adjoint_masked": ([vp, fp, fp, vp, vp, fp, fp, ip, ip, vp], ip),
-        "eff_dots3": ([fp, fp, ctypes.c_longlong, fp, fp, ctypes.c_longlong, vp, vp], ip),
-        "eff_pg_step": ([fp, fp, fp, fp, ip, ip, vp, ip, fp, vp], ip),
+        "eff_dots3": ([fp, fp, ctypes.c_longlong, fp, fp, ctypes.c_longlong, vp, ip, vp], ip),
+        "eff_pg_step": ([fp, fp, fp, fp, ip, ip, vp, ip, fp, fp, ctypes.c_longlong, vp], ip),
         "eff_max_nonneg": ([fp, ctypes.c_longlong, vp, vp], ip),
         "eff_set_cluster_mode": ([ip], ip),
         "eff_batch_create": ([vp, vp, ip, ctypes.POINTER(vp)], ip),
@@ -93,7 +97,10 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "eff_batch_items": ([vp], ip),
         "eff_batch_forward_both": ([vp, vp, vp, vp, vp, vp, vp], ip),
         "eff_batch_adjoint_residual": ([vp, vp, vp, vp, vp, vp, vp, vp, vp], ip),
-        "eff_mu_update": ([fp, fp, fp, ctypes.c_float, ip, ip, ip, ip, vp, ctypes.c_float, vp, vp], ip),
+        "eff_mu_update": ([fp, fp, fp, ctypes.c_float, ip, ip, ip, ip, vp, ctypes.c_float, vp, ip, fp,
+                           ctypes.c_longlong, vp], ip),
+        "eff_forward_ex": ([vp, ip, fp, vp, fp, vp, ip, fp, ctypes.c_longlong, vp, ip, ip, vp], ip),
+        "eff_adjoint_ex": ([vp, fp, fp, fp, vp, vp, fp, fp, vp, ip, ip, ip, vp], ip),
         "eff_loss_grad_static": ([vp, fp, fp, fp, vp, fp, fp, ip, vp], ip),
         "eff_deconv_xdirect": ([vp, fp, vp, vp, fp, fp, ctypes.c_float, ctypes.c_float, ip, vp], ip),
     }

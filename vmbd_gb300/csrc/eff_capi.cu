@@ -27,13 +27,13 @@ cudaError_t launch_basis_project(const float* fs, const float* basis, float* w, 
 cudaError_t launch_edgetaper(float* im, int rows, int cols, const float* wy, int hy, const float* wx,
                              int hx, int batch, cudaStream_t st);
 cudaError_t launch_dots3(const float* a, const float* ap, long long na, const float* b, const float* bp,
-                         long long nb, double* out, cudaStream_t st);
+                         long long nb, double* out, bool zeroed, cudaStream_t st);
 cudaError_t launch_pg_step(float* f, const float* g, float* fp, float* gp, int K, int n, const double* dots,
-                           int mode, float* state, cudaStream_t st);
+                           int mode, float* state, float* zero_f, long long zero_n, cudaStream_t st);
 cudaError_t launch_max_nonneg(const float* a, long long n, unsigned* out_bits, cudaStream_t st);
 cudaError_t launch_mu_update(float* x, const float* num, const float* den, float tol, int rows, int cols,
                              int b0, int b1, const unsigned* num_max_bits, float floor_rel, unsigned* xmax_bits,
-                             cudaStream_t st);
+                             bool zeroed, float* zero_f, long long zero_n, cudaStream_t st);
 }  // namespace eff
 
 struct EffPlan {
@@ -440,6 +440,41 @@ int eff_forward_psf(const EffPlan* plan, const float* f, const void* xhat, float
   return run(plan, eff::OP_FWD_PSF, P, batch, stream);
 }
 
+int eff_forward_ex(const EffPlan* plan, int operand, const float* u, const void* spec, float* y, void* spec_out,
+                   int flags, float* zero_f, long long zero_nf, double* zero_d, int zero_nd, int batch,
+                   void* stream) {
+  if (int s = check_plan(plan, batch)) return s;
+  if (!u || !spec || !y) return fail(EFF_ERR_INVALID, "null argument");
+  if (operand != EFF_OPERAND_IMAGE && operand != EFF_OPERAND_PSF) return fail(EFF_ERR_INVALID, "operand");
+  if ((flags & ~EFF_OUT_ZEROED) || zero_nf < 0 || zero_nd < 0 || (zero_nf > 0 && !zero_f) || (zero_nd > 0 && !zero_d))
+    return fail(EFF_ERR_INVALID, "bad argument");
+  eff::Params P = base_params(plan);
+  if (operand == EFF_OPERAND_IMAGE) P.x = u;
+  else P.f = u;
+  P.b0 = static_cast<const float2*>(spec);
+  P.out0 = y;
+  P.out0_bs = P.y_bs;
+  P.a_out = static_cast<float2*>(spec_out);
+  P.zero_f = zero_nf > 0 ? zero_f : nullptr;
+  P.zero_nf = zero_nf;
+  P.zero_d = zero_nd > 0 ? zero_d : nullptr;
+  P.zero_nd = zero_nd;
+  if (!(flags & EFF_OUT_ZEROED)) {
+    cudaError_t e = cudaMemsetAsync(y, 0, sizeof(float) * P.y_bs * batch, static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+  }
+  return run(plan, operand == EFF_OPERAND_IMAGE ? eff::OP_FWD_IMAGE : eff::OP_FWD_PSF, P, batch, stream);
+}
+
+int eff_adjoint_ex(const EffPlan* plan, const float* y, const float* y_obs, const float* mask, const void* fhat,
+                   const void* xhat, float* gx, float* gf, double* loss, int adj_mode, int flags, int batch,
+                   void* stream) {
+  if (flags & ~EFF_OUT_ZEROED) return fail(EFF_ERR_INVALID, "flags");
+  if (loss && !y_obs) return fail(EFF_ERR_INVALID, "the loss needs y_obs");
+  return adjoint_impl(plan, y, y_obs, fhat, xhat, gx, gf, loss, adj_mode, batch, stream, mask,
+                      (flags & EFF_OUT_ZEROED) != 0);
+}
+
 int eff_adjoint(const EffPlan* plan, const float* y, const void* fhat, const void* xhat, float* gx,
                 float* gf, int adj_mode, int batch, void* stream) {
   return adjoint_impl(plan, y, nullptr, fhat, xhat, gx, gf, nullptr, adj_mode, batch, stream);
@@ -546,19 +581,22 @@ int eff_edgetaper(float* im, int rows, int cols, const float* wy, int hy, const 
 }
 
 int eff_dots3(const float* a, const float* ap, long long na, const float* b, const float* bp, long long nb,
-              double* out, void* stream) {
-  if (!a || !b || !out || na < 1 || nb < 1) return fail(EFF_ERR_INVALID, "bad argument");
-  cudaError_t e = eff::launch_dots3(a, ap, na, b, bp, nb, out, static_cast<cudaStream_t>(stream));
+              double* out, int flags, void* stream) {
+  if (!a || !b || !out || na < 1 || nb < 1 || (flags & ~EFF_OUT_ZEROED)) return fail(EFF_ERR_INVALID, "bad argument");
+  cudaError_t e = eff::launch_dots3(a, ap, na, b, bp, nb, out, (flags & EFF_OUT_ZEROED) != 0,
+                                    static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(e, "dots3 launch");
   return EFF_OK;
 }
 
 int eff_pg_step(float* f, const float* g, float* f_prev, float* g_prev, int K, int n, const double* dots,
-                int mode, float* state, void* stream) {
-  if (!f || !g || !f_prev || !g_prev || !dots || !state || K < 1 || n < 1 || mode < 0 || mode > 2)
+                int mode, float* state, float* zero_f, long long zero_n, void* stream) {
+  if (!f || !g || !f_prev || !g_prev || !dots || !state || K < 1 || n < 1 || mode < 0 || mode > 2 ||
+      zero_n < 0 || (zero_n > 0 && !zero_f))
     return fail(EFF_ERR_INVALID, "bad argument");
   if (n > 12288) return fail(EFF_ERR_UNSUPPORTED, "PSF larger than 12288 samples");
-  cudaError_t e = eff::launch_pg_step(f, g, f_prev, g_prev, K, n, dots, mode, state, static_cast<cudaStream_t>(stream));
+  cudaError_t e = eff::launch_pg_step(f, g, f_prev, g_prev, K, n, dots, mode, state, zero_f, zero_n,
+                                      static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(e, "pg_step launch");
   return EFF_OK;
 }
@@ -571,13 +609,14 @@ int eff_max_nonneg(const float* a, long long n, unsigned* out_bits, void* stream
 }
 
 int eff_mu_update(float* x, const float* num, const float* den, float tol, int rows, int cols, int border0,
-                  int border1, const unsigned* num_max_bits, float floor_rel, unsigned* xmax_bits,
-                  void* stream) {
+                  int border1, const unsigned* num_max_bits, float floor_rel, unsigned* xmax_bits, int flags,
+                  float* zero_f, long long zero_n, void* stream) {
   if (!x || !num || !den || !xmax_bits || !num_max_bits || rows < 1 || cols < 1 || border0 < 0 ||
-      border1 < 0 || !(floor_rel >= 0.f))
+      border1 < 0 || !(floor_rel >= 0.f) || (flags & ~EFF_OUT_ZEROED) || zero_n < 0 || (zero_n > 0 && !zero_f))
     return fail(EFF_ERR_INVALID, "bad argument");
   cudaError_t e = eff::launch_mu_update(x, num, den, tol, rows, cols, border0, border1, num_max_bits,
-                                        floor_rel, xmax_bits, static_cast<cudaStream_t>(stream));
+                                        floor_rel, xmax_bits, (flags & EFF_OUT_ZEROED) != 0, zero_f, zero_n,
+                                        static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(e, "mu_update launch");
   return EFF_OK;
 }

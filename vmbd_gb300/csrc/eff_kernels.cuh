@@ -746,7 +746,7 @@ __device__ __forceinline__ void zero_next(const Params& P) {
 template <int N, int OP, int CL>
 __global__ void __launch_bounds__(max_threads(N)) eff_kernel(Params P) {
   extern __shared__ __align__(16) float2 smem[];
-  if constexpr (OP == OP_FWD_BOTH) zero_next(P);
+  if constexpr (OP == OP_FWD_BOTH || OP == OP_FWD_IMAGE || OP == OP_FWD_PSF) zero_next(P);
   eff_patch<N, OP, CL>(P, blockIdx.x / CL, blockIdx.y, smem, blockIdx.x, gridDim.x);
 }
 

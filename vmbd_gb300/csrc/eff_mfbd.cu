@@ -92,13 +92,22 @@ __device__ __forceinline__ float pg_step_size(const double* dots, int mode, floa
   return (float)s;
 }
 
+// Side job of a kernel: zero [z, z + nz) (a buffer a later call accumulates
+// into and that this kernel neither reads nor writes otherwise), grid-stride.
+__device__ __forceinline__ void zero_side(float* z, long long nz) {
+  if (!z) return;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nz; t += (long long)gridDim.x * blockDim.x)
+    z[t] = 0.f;
+}
+
 // One PSF per CTA: fp <- f, gp <- g, f <- P_simplex(f - s g).  state[0] holds
 // the step size (written by CTA 0).
 __global__ void __launch_bounds__(kMfbdThreads) pg_step_kernel(float* f, const float* g, float* fp, float* gp,
                                                                int n, const double* dots, int mode,
-                                                               float* state) {
+                                                               float* state, float* zero_f, long long zero_n) {
   extern __shared__ float v[];
   __shared__ float2 red[32];
+  zero_side(zero_f, zero_n);
   const float s = pg_step_size(dots, mode, state[0]);
   const long long base = (long long)blockIdx.x * n;
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
@@ -172,7 +181,8 @@ __global__ void __launch_bounds__(kMfbdThreads) max_nonneg_kernel(const float* a
 __global__ void __launch_bounds__(kMfbdThreads) mu_update_kernel(float* x, const float* num, const float* den,
                                                                  float tol, int rows, int cols, int b0, int b1,
                                                                  const unsigned* num_max_bits, float floor_rel,
-                                                                 unsigned* xmax_bits) {
+                                                                 unsigned* xmax_bits, float* zero_f, long long zero_n) {
+  zero_side(zero_f, zero_n);
   const long long n = (long long)rows * cols;
   const float nfloor = floor_rel * __uint_as_float(*num_max_bits);
   float m = 0.f;
@@ -203,16 +213,18 @@ static int grid_for(long long n) {
 }
 
 cudaError_t launch_dots3(const float* a, const float* ap, long long na, const float* b, const float* bp,
-                         long long nb, double* out, cudaStream_t st) {
-  cudaError_t e = cudaMemsetAsync(out, 0, 3 * sizeof(double), st);
-  if (e != cudaSuccess) return e;
+                         long long nb, double* out, bool zeroed, cudaStream_t st) {
+  if (!zeroed) {
+    cudaError_t e = cudaMemsetAsync(out, 0, 3 * sizeof(double), st);
+    if (e != cudaSuccess) return e;
+  }
   dots3_kernel<<<grid_for(na > nb ? na : nb), kMfbdThreads, 0, st>>>(a, ap, na, b, bp, nb, out);
   return cudaGetLastError();
 }
 
 cudaError_t launch_pg_step(float* f, const float* g, float* fp, float* gp, int K, int n, const double* dots,
-                           int mode, float* state, cudaStream_t st) {
-  pg_step_kernel<<<K, kMfbdThreads, n * sizeof(float), st>>>(f, g, fp, gp, n, dots, mode, state);
+                           int mode, float* state, float* zero_f, long long zero_n, cudaStream_t st) {
+  pg_step_kernel<<<K, kMfbdThreads, n * sizeof(float), st>>>(f, g, fp, gp, n, dots, mode, state, zero_f, zero_n);
   return cudaGetLastError();
 }
 
@@ -225,12 +237,12 @@ cudaError_t launch_max_nonneg(const float* a, long long n, unsigned* out_bits, c
 
 cudaError_t launch_mu_update(float* x, const float* num, const float* den, float tol, int rows, int cols,
                              int b0, int b1, const unsigned* num_max_bits, float floor_rel, unsigned* xmax_bits,
-                             cudaStream_t st) {
-  cudaError_t e = cudaMemsetAsync(xmax_bits, 0, sizeof(unsigned), st);
-  if (e != cudaSuccess) return e;
+                             bool zeroed, float* zero_f, long long zero_n, cudaStream_t st) {
+  cudaError_t e;
+  if (!zeroed && (e = cudaMemsetAsync(xmax_bits, 0, sizeof(unsigned), st)) != cudaSuccess) return e;
   const long long n = (long long)rows * cols;
   mu_update_kernel<<<grid_for(n), kMfbdThreads, 0, st>>>(x, num, den, tol, rows, cols, b0, b1, num_max_bits,
-                                                          floor_rel, xmax_bits);
+                                                          floor_rel, xmax_bits, zero_f, zero_n);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   clamp_max_kernel<<<grid_for(n), kMfbdThreads, 0, st>>>(x, n, xmax_bits);
   return cudaGetLastError();

@@ -77,5 +77,5 @@ def dots3(a, b, ap=None, bp=None):
     """(sum u^2, sum u v, sum v^2) with u = a - ap, v = b - bp, in FP64."""
     out = torch.empty(3, dtype=torch.float64, device=a.device)
     _lib.check(_lib.load().eff_dots3(_ptr(a), _ptr(ap), a.numel(), _ptr(b), _ptr(bp), b.numel(),
-                                     _ptr(out), _stream(a.device)))
+                                     _ptr(out), 0, _stream(a.device)))
     return out

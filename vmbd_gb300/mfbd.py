@@ -70,10 +70,14 @@ class OnlineMFBD:
         self.ypred = z(self.sy)
         self.yg = z(self.sy)
         self.num = z(self.sx)
-        self.den = z(self.sx)
+        nx = self.sx[0] * self.sx[1]
+        # den and the interior-maximum word share one buffer, so that one
+        # side job of the image forward clears both
+        self._denx = z(nx + 1)
+        self.den = self._denx[:nx].view(self.sx)
         self.dots = z(3, torch.float64)
         self.state = torch.ones(1, dtype=torch.float32, device=dev)
-        self.xmax = z(1, torch.int32)
+        self.xmax = self._denx[nx:].view(torch.int32)
         self.nummax = z(1, torch.int32)
         self.taper = EdgeTaper(self.sf, dev) if taper else None
 
@@ -97,38 +101,54 @@ class OnlineMFBD:
         torch.lt(self.y, 1.0, out=self.mask)  # bool -> float via out dtype
         K, n = self.winaux.K, self.n
         ny = self.sy[0] * self.sy[1]
+        # Accumulated outputs are cleared as side jobs of earlier kernels that
+        # do not touch them (EFF_OUT_ZEROED on their own call), so the frame
+        # graph has three memset nodes instead of ~40.
+        OZ, nx = _lib.OUT_ZEROED, self.sx[0] * self.sx[1]
+        amode = _lib.ADJ_EXACT if self.adjoint == "exact" else _lib.ADJ_REFERENCE
         # --- PSF estimation: X object of the current latent image --------
         P.image_spectrum(self.x, out=self.xhat)
         for k in range(self.n_pg):
-            P.forward_psf(self.f, self.xhat, out=self.ypred)
-            # the BB / exact-line-search steps need no objective value: no loss reduction
-            P.adjoint_residual(self.ypred, self.y, xhat=self.xhat, want_image=False, gf=self.g,
-                               want_loss=False, adjoint=self.adjoint)
+            # y_pred = X f (y_pred cleared by the previous PSF step; memset at
+            # k = 0); side jobs: clear dots (and yg at k = 0)
+            self._check(L.eff_forward_ex(P._h, _lib.OPERAND_PSF, _ptr(self.f), _ptr(self.xhat), _ptr(self.ypred),
+                                         None, OZ if k > 0 else 0, _ptr(self.yg) if k == 0 else None,
+                                         ny if k == 0 else 0, _ptr(self.dots), 3, 1, st))
+            # g = X^T (y_pred - y); the BB / exact-line-search steps need no objective value
+            self._check(L.eff_adjoint_ex(P._h, _ptr(self.ypred), _ptr(self.y), None, None, _ptr(self.xhat),
+                                         None, _ptr(self.g), None, amode, 0, 1, st))
             if k == 0:
-                P.forward_psf(self.g, self.xhat, out=self.yg)
+                self._check(L.eff_forward_ex(P._h, _lib.OPERAND_PSF, _ptr(self.g), _ptr(self.xhat),
+                                             _ptr(self.yg), None, OZ, None, 0, None, 0, 1, st))
                 self._check(L.eff_dots3(_ptr(self.g), None, K * n, _ptr(self.yg), None, ny,
-                                        _ptr(self.dots), st))
+                                        _ptr(self.dots), OZ, st))
                 mode = 0
             else:
                 self._check(L.eff_dots3(_ptr(self.f), _ptr(self.f_prev), K * n, _ptr(self.g),
-                                        _ptr(self.g_prev), K * n, _ptr(self.dots), st))
+                                        _ptr(self.g_prev), K * n, _ptr(self.dots), OZ, st))
                 mode = 1 if k % 2 == 1 else 2
+            # side job: clear y_pred for the next forward
             self._check(L.eff_pg_step(_ptr(self.f), _ptr(self.g), _ptr(self.f_prev), _ptr(self.g_prev),
-                                      K, n, _ptr(self.dots), mode, _ptr(self.state), st))
+                                      K, n, _ptr(self.dots), mode, _ptr(self.state), _ptr(self.ypred), ny, st))
         # --- latent image: F object of the new PSFs ------------------------
         P.psf_spectrum(self.f, out=self.fhat)
-        mode = _lib.ADJ_EXACT if self.adjoint == "exact" else _lib.ADJ_REFERENCE
         self._check(L.eff_adjoint_masked(P._h, _ptr(self.y), _ptr(self.mask), _ptr(self.fhat), None,
-                                         _ptr(self.num), None, mode, 1, st))
-        self._check(L.eff_max_nonneg(_ptr(self.num), self.sx[0] * self.sx[1], _ptr(self.nummax), st))
-        for _ in range(self.n_mu):
-            P.forward_image(self.x, self.fhat, out=self.ypred)
-            self._check(L.eff_adjoint_masked(P._h, _ptr(self.ypred), _ptr(self.mask), _ptr(self.fhat),
-                                             None, _ptr(self.den), None, mode, 1, st))
+                                         _ptr(self.num), None, amode, 1, st))
+        self._check(L.eff_max_nonneg(_ptr(self.num), nx, _ptr(self.nummax), st))
+        for i in range(self.n_mu):
+            # y_pred = F x (y_pred cleared by the previous PSF step or image
+            # step); side job: clear den and the interior-maximum word
+            self._check(L.eff_forward_ex(P._h, _lib.OPERAND_IMAGE, _ptr(self.x), _ptr(self.fhat),
+                                         _ptr(self.ypred), None, OZ if (i > 0 or self.n_pg > 0) else 0,
+                                         _ptr(self._denx), nx + 1, None, 0, 1, st))
+            self._check(L.eff_adjoint_ex(P._h, _ptr(self.ypred), None, _ptr(self.mask), _ptr(self.fhat), None,
+                                         _ptr(self.den), None, None, amode, OZ, 1, st))
+            last = i == self.n_mu - 1
             self._check(L.eff_mu_update(_ptr(self.x), _ptr(self.num), _ptr(self.den),
                                         ctypes.c_float(self.tol), self.sx[0], self.sx[1], self.sf[0],
                                         self.sf[1], _ptr(self.nummax), ctypes.c_float(self.NUM_FLOOR),
-                                        _ptr(self.xmax), st))
+                                        _ptr(self.xmax), OZ, None if last else _ptr(self.ypred),
+                                        0 if last else ny, st))
 
     def launches_per_frame(self) -> int:
         """Kernels of this library one frame launches."""
