@@ -343,13 +343,17 @@ def profile_run(args, dev):
         print(json.dumps({"profile": "deconv", "steps": args.warmup + args.steps}))
         return
     if args.workload == "cfg4":
-        from vmbd_gb300.eff import EffBatch
+        # one autotuner candidate (--candidate), eagerly, without the tuning runs
+        from vmbd_gb300 import autotune
         plans, counts, xs, fs, yo = cfg4_data(dev)
-        B = EffBatch(plans, counts)
+        runner = autotune.BatchRunner(plans, counts, args.candidate)
+        losses = [torch.empty(c, dtype=torch.float64, device=dev) for c in counts]
+        gxs = [torch.empty((c,) + p.sx, device=dev) for p, c in zip(plans, counts)]
+        gfs = [torch.empty((c, p.K) + p.sf, device=dev) for p, c in zip(plans, counts)]
         for _ in range(args.warmup + args.steps):
-            B.loss_grad(xs, fs, yo)
+            runner.loss_grad(xs, fs, yo, losses, gxs, gfs)
         torch.cuda.synchronize(dev)
-        print(json.dumps({"profile": "cfg4", "steps": args.warmup + args.steps}))
+        print(json.dumps({"profile": "cfg4", "candidate": args.candidate, "steps": args.warmup + args.steps}))
         return
     w = WORKLOADS[args.workload]
     wa, x_np, f_np = make_inputs(w, seed=0)
@@ -599,6 +603,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=list(WORKLOADS) + ["mfbd", "cfg4", "deconv"], default="cfg2")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--candidate", default="persistent",
+                    help="uneven-batch strategy for --workload cfg4 --profile (an autotuner candidate)")
     ap.add_argument("--profile", action="store_true",
                     help="short eager run of the step only (for an ncu launch list / capture)")
     args = ap.parse_args()

@@ -366,3 +366,50 @@ def test_reference_error_behaviour(cuda):
     F = OlaGPU(f, (96, 96), "valid", wa)
     with pytest.raises(IOError):
         F.cnv(np.zeros((95, 96), np.float32))
+
+
+def test_chained_call_entry_points(cuda):
+    """eff_forward_ex / eff_adjoint_ex: the same results as the plain entry
+    points, outputs taken as already zero when flagged, and the side-job
+    buffers cleared."""
+    import ctypes
+    import torch
+    from vmbd_gb300 import _lib
+    from vmbd_gb300.eff import EffPlan, _ptr
+    wa, g, x, f, r = make(**CASES["cfg1_literal"])
+    plan = EffPlan(wa, g.sf, g.mode, device=cuda)
+    L = _lib.load()
+    st = ctypes.c_void_p(torch.cuda.current_stream(cuda).cuda_stream)
+    xt, ft, rt = t(x, cuda), t(f, cuda), t(r, cuda)
+    fh, xh = plan.psf_spectrum(ft), plan.image_spectrum(xt)
+    y_img = plan.forward_image(xt, fh)
+    y_psf = plan.forward_psf(ft, xh)
+    for operand, u, spec, want in ((_lib.OPERAND_IMAGE, xt, fh, y_img), (_lib.OPERAND_PSF, ft, xh, y_psf)):
+        for flags in (0, _lib.OUT_ZEROED):
+            y = torch.zeros_like(want) if flags else torch.full_like(want, 7.0)
+            side_f = torch.ones(12345, device=cuda)
+            side_d = torch.ones(3, dtype=torch.float64, device=cuda)
+            _lib.check(L.eff_forward_ex(plan._h, operand, _ptr(u), _ptr(spec), _ptr(y), None, flags, _ptr(side_f),
+                                        side_f.numel(), _ptr(side_d), 3, 1, st))
+            assert rel(y.cpu(), want.cpu()) < 1e-6
+            assert not side_f.any() and not side_d.any()
+    mask = (torch.rand(plan.sy, device=cuda, generator=torch.Generator(device=cuda).manual_seed(3)) > 0.3).float()
+    gx_ref, _ = plan.adjoint(rt * mask, fh, xh, want_psf=False)
+    yo = 0.5 * rt
+    loss_ref, _, gf_ref = plan.adjoint_residual(rt, yo, fh, xh, want_image=False)
+    for flags in (0, _lib.OUT_ZEROED):
+        gx = torch.zeros(plan.sx, device=cuda) if flags else torch.full(plan.sx, 3.0, device=cuda)
+        _lib.check(L.eff_adjoint_ex(plan._h, _ptr(rt), None, _ptr(mask), _ptr(fh), None, _ptr(gx), None, None,
+                                    _lib.ADJ_EXACT, flags, 1, st))
+        assert rel(gx.cpu(), gx_ref.cpu()) < 1e-6
+        loss = torch.zeros((), dtype=torch.float64, device=cuda) if flags else torch.ones((), dtype=torch.float64,
+                                                                                          device=cuda)
+        gf = torch.empty((plan.K,) + plan.sf, device=cuda)
+        _lib.check(L.eff_adjoint_ex(plan._h, _ptr(rt), _ptr(yo), None, None, _ptr(xh), None, _ptr(gf),
+                                    _ptr(loss), _lib.ADJ_EXACT, flags, 1, st))
+        assert rel(gf.cpu(), gf_ref.cpu()) < 1e-6
+        assert abs(float(loss) - float(loss_ref)) < 1e-6 * float(loss_ref)
+    assert L.eff_forward_ex(plan._h, 5, _ptr(xt), _ptr(fh), _ptr(y_img), None, 0, None, 0, None, 0, 1, st) \
+        == _lib.EFF_ERR_INVALID
+    assert L.eff_adjoint_ex(plan._h, _ptr(rt), None, None, _ptr(fh), None, _ptr(gx_ref), None, None,
+                            _lib.ADJ_EXACT, 4, 1, st) == _lib.EFF_ERR_INVALID

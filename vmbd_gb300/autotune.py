@@ -5,7 +5,8 @@ device.
 A candidate is ``strategy[@f<frame>][/t<threads>]``:
 
 * strategy ``persistent``: one persistent launch per direction over all
-  classes (``EffBatch``; 2-CTA clusters, 256 threads per CTA);
+  classes (``EffBatch``; 2-CTA clusters, 512 threads per CTA, one CTA per
+  SM -- shared memory is sized for the largest frame of the mix);
   ``per_class/cta``: one batched launch per class and direction, one CTA per
   patch; ``per_class/cluster``: the same with a 2-CTA cluster per patch;
 * ``@f192``: classes whose convolution extent fits run on the 192 frame

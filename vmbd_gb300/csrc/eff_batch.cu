@@ -20,7 +20,7 @@
 namespace eff {
 
 constexpr int kMaxClasses = 8;
-constexpr int kBatchThreads = 256;
+constexpr int kBatchThreads = 512;
 
 // Defined with the plan (eff_capi.cu): the plan's kernel parameters with no
 // data pointers, its frame edge, and its patch count.
