@@ -59,7 +59,7 @@ typedef struct EffGeom {
   int csf[2];  /* patch grid */
   int sw[2];   /* patch size */
   int hop[2];  /* patch hop */
-  int sfft;    /* FFT frame edge, 64, 128, 192 or 256 (>= max(E)); 0 = the smallest power of two >= max(E) */
+  int sfft;    /* FFT frame edge, 64, 128, 192, 256 or 512 (>= max(E)); 0 = the smallest power of two >= max(E) */
   int mode;    /* EFF_MODE_* */
   int threads; /* CTA size, a multiple of 32 up to 512 (384 for the 192 frame); 0 = the
                   largest that fits.  Lowered to fit shared memory. */

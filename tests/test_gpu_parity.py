@@ -93,12 +93,17 @@ CASES = {
     "cfg1_literal_f192": dict(sx=(256, 256), csf=(4, 4), sf=(15, 15), sw=(64, 64), hop=(32, 32), sfft=192),
     "same_mode": dict(sx=(200, 232), csf=(3, 4), sf=(12, 10), mode="same"),
     "full_mode": dict(sx=(200, 232), csf=(3, 4), sf=(12, 10), mode="full"),
+    # frame 512 (32 values per lane): extent 292 on 4-CTA clusters, 424 on 8-CTA clusters
+    "frame512_cl4": dict(sx=(400, 400), csf=(2, 2), sf=(25, 25), kind="motion"),
+    "frame512_cl8": dict(sx=(600, 600), csf=(2, 2), sf=(25, 25), kind="motion"),
+    "frame512_same": dict(sx=(400, 440), csf=(2, 2), sf=(25, 21), mode="same"),
     "full_mode_f192": dict(sx=(200, 232), csf=(3, 4), sf=(12, 10), mode="full", sfft=192),
 }
 # frame each case runs on
 FRAME = {"cfg1_literal": 128, "cfg1_winaux": 128, "cfg2_literal": 128, "cfg2_winaux": 256,
          "cfg2_winaux_f192": 192, "cfg3_winaux": 256, "cfg3_winaux_f192": 192, "cfg4_mixed": 256,
-         "cfg4_mixed_f192": 192, "cfg1_literal_f192": 192}
+         "cfg4_mixed_f192": 192, "cfg1_literal_f192": 192, "frame512_cl4": 512, "frame512_cl8": 512,
+         "frame512_same": 512}
 
 
 @pytest.fixture(params=[1, 2], ids=["cta", "cluster2"])
@@ -164,6 +169,25 @@ def test_2048_stress_workload(cuda):
                           kind="motion", seed=21)
     plan = EffPlan(wa, g.sf, device=cuda)
     assert plan.N == 256
+    xh, fh = plan.empty_spectrum(), plan.empty_spectrum()
+    y = plan.forward_both(t(x, cuda), t(f, cuda), xhat_out=xh, fhat_out=fh)
+    assert rel(y.cpu().numpy(), eff64.forward(x, f, g, wa.ws.astype(np.float64))) < TOL
+    gx, gf = plan.adjoint(t(r, cuda), fh, xh)
+    lhs = np.vdot(y.double().cpu().numpy(), r)
+    assert abs(lhs - np.vdot(x, gx.double().cpu().numpy())) < 1e-5 * abs(lhs)
+    assert abs(lhs - np.vdot(f, gf.double().cpu().numpy())) < 1e-5 * abs(lhs)
+
+
+def test_2048_winaux_stress_workload(cuda):
+    """The stress image on win2winaux's own geometry: 2088x2088 (valid output
+    2048x2048), 16x16 grid of 246x246 patches (hop 123), 41x41 motion PSFs,
+    extent 286: frame 512 on 4-CTA clusters.  Forward against the FP64
+    oracle at full size; both adjoints through the adjoint identity."""
+    from vmbd_gb300.eff import EffPlan
+    wa, g, x, f, r = make(sx=(2088, 2088), csf=(16, 16), sf=(41, 41), kind="motion", seed=23)
+    assert tuple(wa.sw) == (246, 246)
+    plan = EffPlan(wa, g.sf, device=cuda)
+    assert plan.N == 512
     xh, fh = plan.empty_spectrum(), plan.empty_spectrum()
     y = plan.forward_both(t(x, cuda), t(f, cuda), xhat_out=xh, fhat_out=fh)
     assert rel(y.cpu().numpy(), eff64.forward(x, f, g, wa.ws.astype(np.float64))) < TOL

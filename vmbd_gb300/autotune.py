@@ -9,9 +9,9 @@ A candidate is ``strategy[@f<frame>][/t<threads>]``:
   SM -- shared memory is sized for the largest frame of the mix);
   ``per_class/cta``: one batched launch per class and direction, one CTA per
   patch; ``per_class/cluster``: the same with a 2-CTA cluster per patch;
-* ``@f192``: classes whose convolution extent fits run on the 192 frame
-  (24 x 8 mixed radix, ~45% less arithmetic than 256, longer per-lane
-  chains) instead of their power-of-two frame;
+* ``@f192``: classes on the 256 frame whose convolution extent fits run on
+  the 192 frame (24 x 8 mixed radix, ~45% less arithmetic, longer per-lane
+  chains);
 * ``t<n>`` (after ``@``, ``/``-separated from ``f``): CTA size of the
   per-class launches (default: the largest that fits).
 
@@ -54,11 +54,11 @@ def _extent(p):
 
 
 def variant_plans(plans, frame: int = 0, threads: int = 0):
-    """The class plans on another frame (classes it fits; others unchanged)
-    and/or CTA size."""
+    """The class plans on a smaller frame (the classes whose extent fits it
+    and whose own frame is larger; others unchanged) and/or CTA size."""
     out = []
     for p in plans:
-        n = frame if frame and _extent(p) <= frame else p.N
+        n = frame if frame and _extent(p) <= frame < p.N else p.N
         if n == p.N and not threads:
             out.append(p)
         else:

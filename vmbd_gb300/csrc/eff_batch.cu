@@ -123,6 +123,8 @@ int eff_batch_create(const EffPlan* const* plans, const int* counts, int n_class
     B.counts[c] = counts[c];
     int n = 0;
     eff_plan_frame(plans[c], &n);
+    if (n == 512)  // its patches need clusters of 4-8 CTAs, the persistent grid has pairs
+      return fail(EFF_ERR_UNSUPPORTED, "frame 512 is not supported in a persistent batch");
     order.push_back({-n, c});
   }
   std::stable_sort(order.begin(), order.end());

@@ -42,7 +42,8 @@ struct EffPlan {
   int K;
   int sy[2], off[2], E[2];
   int threads;   // per CTA when one CTA handles a patch
-  int threads2;  // per CTA of a 2-CTA cluster
+  int threads2;  // per CTA of a 2-CTA cluster (frame 512: of a clw-CTA cluster)
+  int clw;       // frame 512: CTAs per patch (4, or 8 when a quarter frame does not fit)
   int num_sms;
   int device;
   float2* win0;
@@ -72,8 +73,8 @@ int cuda_fail(cudaError_t e, const char* what) {
 // its 24 values per lane make each lane's dependent chain ~1.5x longer, which
 // costs more than its ~45% less arithmetic saves on latency-bound single
 // images; batches that fill the GPU can gain (the batch autotuner tries it).
-constexpr int kFrames[] = {64, 128, 256};
-int frame_ok(int n) { return n == 64 || n == 128 || n == 192 || n == 256; }
+constexpr int kFrames[] = {64, 128, 256, 512};
+int frame_ok(int n) { return n == 64 || n == 128 || n == 192 || n == 256 || n == 512; }
 
 eff::Params base_params(const EffPlan* p) {
   eff::Params P;
@@ -104,14 +105,16 @@ int run(const EffPlan* p, int op, const eff::Params& P, int batch, void* stream)
   const size_t smem2 = eff::smem_bytes(p->N, op, P, p->threads2, 2);
   // A 2-CTA cluster per patch when one CTA's frame does not fit, or when the
   // doubled grid still fits in one wave (more SMs on a small launch).
+  // Frame 512 always runs on its clw-CTA clusters.
   const int mode = g_cluster_mode.load();
   int CL;
-  if (smem1 > kSmemLimit) CL = 2;
+  if (p->N == 512) CL = p->clw;
+  else if (smem1 > kSmemLimit) CL = 2;
   else if (mode == 1) CL = 1;
   else if (mode == 2) CL = 2;
   else CL = (2LL * p->K * batch <= p->num_sms) ? 2 : 1;
-  const size_t smem = CL == 2 ? smem2 : smem1;
-  const int threads = CL == 2 ? p->threads2 : p->threads;
+  const size_t smem = CL == 1 ? smem1 : (CL == 2 ? smem2 : eff::smem_bytes(p->N, op, P, p->threads2, CL));
+  const int threads = CL == 1 ? p->threads : p->threads2;
   if (smem > kSmemLimit)
     return fail(EFF_ERR_UNSUPPORTED, "frame needs " + std::to_string(smem) + " bytes of shared memory");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
@@ -121,6 +124,7 @@ int run(const EffPlan* p, int op, const eff::Params& P, int batch, void* stream)
     case 128: e = eff::launch_n128(op, CL, P, p->K, batch, threads, smem, st); break;
     case 192: e = eff::launch_n192(op, CL, P, p->K, batch, threads, smem, st); break;
     case 256: e = eff::launch_n256(op, CL, P, p->K, batch, threads, smem, st); break;
+    case 512: e = eff::launch_n512(op, CL, P, p->K, batch, threads, smem, st); break;
     default: return fail(EFF_ERR_UNSUPPORTED, "frame size");
   }
   if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
@@ -274,13 +278,13 @@ int eff_plan_create(const EffGeom* geom, const float* win0, const float* win1, E
         p.N = n;
         break;
       }
-    if (p.N == 0) p.N = 512;  // rejected below
+    if (p.N == 0) p.N = 1024;  // rejected below
   } else {
     p.N = g.sfft;
   }
   if (!frame_ok(p.N))
     return fail(EFF_ERR_UNSUPPORTED, "FFT frame " + std::to_string(p.N) +
-                                         " (needs 64, 128, 192 or 256, >= sw + sf - 1 = " +
+                                         " (needs 64, 128, 192, 256 or 512, >= sw + sf - 1 = " +
                                          std::to_string(emax) + ")");
   if (p.N < emax) return fail(EFF_ERR_INVALID, "FFT frame smaller than sw + sf - 1");
   if (g.threads != 0 && (g.threads < 32 || g.threads % 32 != 0 || g.threads > eff::max_threads(p.N)))
@@ -316,6 +320,33 @@ int eff_plan_create(const EffGeom* geom, const float* win0, const float* win1, E
       }
       if (worst <= kSmemLimit || p.threads2 <= 128) break;
       p.threads2 = (p.threads2 / 2 + 31) / 32 * 32;
+    }
+    // Frame 512 runs on clusters of 4 CTAs (each a quarter of the half
+    // spectrum), or of 8 when a quarter frame does not fit; the CTA size is
+    // halved while it does not fit.
+    if (p.N == 512) {
+      p.clw = 0;
+      for (int cl : {4, 8}) {
+        int t = g.threads ? g.threads : eff::max_threads(p.N);
+        size_t worst = 0;
+        for (;;) {
+          worst = 0;
+          for (int op = 0; op < eff::kNumOps; ++op) {
+            const size_t s = eff::smem_bytes(p.N, op, P, t, cl);
+            if (s > worst) worst = s;
+          }
+          if (worst <= kSmemLimit || t <= 64) break;
+          t = (t / 2 + 31) / 32 * 32;
+        }
+        if (worst <= kSmemLimit) {
+          p.clw = cl;
+          p.threads2 = t;
+          break;
+        }
+      }
+      if (p.clw == 0)
+        return fail(EFF_ERR_UNSUPPORTED, "frame 512: the frame rows (sw + sf - 1 = " + std::to_string(emax) +
+                                             ") do not fit in shared memory even split over 8 CTAs");
     }
   }
 

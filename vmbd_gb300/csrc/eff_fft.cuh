@@ -1,8 +1,8 @@
 // Register / sub-warp FFT building blocks for the EFF kernels (sm_103a).
 //
 // A length-N complex FFT (N = R*G: N = 64, 128, 256 with R = 16 values per
-// lane; N = 192 with R = 24) is computed by a group of G consecutive lanes of
-// one warp, each lane holding R values:
+// lane; N = 192 with R = 24; N = 512 with R = 32) is computed by a group of G
+// consecutive lanes of one warp, each lane holding R values:
 //
 //   layout "A": lane g, register m  <->  element g + G*m.
 //
@@ -14,7 +14,7 @@
 // conjugate twiddles (unnormalised).
 //
 // Arithmetic is FP32; the in-register twiddles are exact decimal expansions of
-// cos/sin(2*pi*j/48) and the W_N table is computed in FP64 on the host.
+// cos/sin(2*pi*j/96) and the W_N table is computed in FP64 on the host.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -32,39 +32,52 @@ __device__ __forceinline__ float2 cmulc(float2 a, float2 b) {
 }
 __device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
 
-// cos / sin of 2*pi*j/48.
-__host__ __device__ constexpr float cos48_q(int j) {  // j in [0, 12]
+// cos / sin of 2*pi*j/96 (the grid of every in-register twiddle: the radix-2
+// stages up to 32 points and the 3 x 8 factorisation of 24).
+__host__ __device__ constexpr float cos96_q(int j) {  // j in [0, 24]
   switch (j) {
     case 0: return 1.f;
-    case 1: return 0.99144486137381041f;
-    case 2: return 0.96592582628906829f;
-    case 3: return 0.92387953251128674f;
-    case 4: return 0.86602540378443865f;
-    case 5: return 0.79335334029123517f;
-    case 6: return 0.70710678118654752f;
-    case 7: return 0.60876142900872066f;
-    case 8: return 0.5f;
-    case 9: return 0.38268343236508978f;
-    case 10: return 0.25881904510252076f;
-    case 11: return 0.13052619222005159f;
+    case 1: return 0.9978589232386035067f;
+    case 2: return 0.9914448613738104111f;
+    case 3: return 0.9807852804032304491f;
+    case 4: return 0.9659258262890682867f;
+    case 5: return 0.9469301294951056642f;
+    case 6: return 0.9238795325112867561f;
+    case 7: return 0.8968727415326883038f;
+    case 8: return 0.8660254037844386467f;
+    case 9: return 0.8314696123025452370f;
+    case 10: return 0.7933533402912351645f;
+    case 11: return 0.7518398074789773964f;
+    case 12: return 0.7071067811865475244f;
+    case 13: return 0.6593458151000688684f;
+    case 14: return 0.6087614290087206394f;
+    case 15: return 0.5555702330196022247f;
+    case 16: return 0.5f;
+    case 17: return 0.4422886902190012819f;
+    case 18: return 0.3826834323650897717f;
+    case 19: return 0.3214394653031615807f;
+    case 20: return 0.2588190451025207623f;
+    case 21: return 0.1950903220161282678f;
+    case 22: return 0.1305261922200515915f;
+    case 23: return 0.0654031292301430668f;
     default: return 0.f;
   }
 }
-__host__ __device__ constexpr float cos48(int j) {
-  j = ((j % 48) + 48) % 48;
-  return j <= 12 ? cos48_q(j) : (j <= 24 ? -cos48_q(24 - j) : (j <= 36 ? -cos48_q(j - 24) : cos48_q(48 - j)));
+__host__ __device__ constexpr float cos96(int j) {
+  j = ((j % 96) + 96) % 96;
+  return j <= 24 ? cos96_q(j) : (j <= 48 ? -cos96_q(48 - j) : (j <= 72 ? -cos96_q(j - 48) : cos96_q(96 - j)));
 }
-__host__ __device__ constexpr float sin48(int j) { return cos48(j - 12); }
+__host__ __device__ constexpr float sin96(int j) { return cos96(j - 24); }
 
-// v * W where W = exp(-+ 2*pi*i * e48/48) (forward: minus, INV: plus).
+// v * W where W = exp(-+ 2*pi*i * e/96) (forward: minus, INV: plus).
 template <bool INV>
-__device__ __forceinline__ float2 twiddle48(float2 v, int e48) {
-  e48 = ((e48 % 48) + 48) % 48;
-  if (e48 == 0) return v;
-  if (e48 == 24) return make_float2(-v.x, -v.y);
-  if (e48 == 12) return INV ? make_float2(-v.y, v.x) : make_float2(v.y, -v.x);
-  if (e48 == 36) return INV ? make_float2(v.y, -v.x) : make_float2(-v.y, v.x);
-  const float c = cos48(e48), s = sin48(e48);
+__device__ __forceinline__ float2 twiddle96(float2 v, int e) {
+  e = ((e % 96) + 96) % 96;
+  if (e == 0) return v;
+  if (e == 48) return make_float2(-v.x, -v.y);
+  if (e == 24) return INV ? make_float2(-v.y, v.x) : make_float2(v.y, -v.x);
+  if (e == 72) return INV ? make_float2(v.y, -v.x) : make_float2(-v.y, v.x);
+  const float c = cos96(e), s = sin96(e);
   if (INV) return make_float2(fmaf(v.x, c, -v.y * s), fmaf(v.y, c, v.x * s));
   return make_float2(fmaf(v.x, c, v.y * s), fmaf(v.y, c, -v.x * s));
 }
@@ -78,7 +91,7 @@ __host__ __device__ constexpr int bitrev(int i, int R) {
   return r;
 }
 
-// In-register DFT of a power-of-two size R (2..16), natural order in and
+// In-register DFT of a power-of-two size R (2..32), natural order in and
 // out: iterative radix-2 decimation in time; every index is a compile-time
 // constant after unrolling, so the bit reversal is register renaming.
 template <int R, bool INV>
@@ -93,7 +106,7 @@ __device__ __forceinline__ void dft_pow2(float2 (&a)[R]) {
 #pragma unroll
       for (int j = 0; j < len / 2; ++j) {
         const float2 u = b[i + j];
-        const float2 v = twiddle48<INV>(b[i + j + len / 2], j * (48 / len));
+        const float2 v = twiddle96<INV>(b[i + j + len / 2], j * (96 / len));
         b[i + j] = cadd(u, v);
         b[i + j + len / 2] = csub(u, v);
       }
@@ -126,8 +139,8 @@ __device__ __forceinline__ void dft24(float2 (&a)[24]) {
     float2 p = a[n2], q = a[8 + n2], r = a[16 + n2];
     dft3<INV>(p, q, r);
     y[0][n2] = p;
-    y[1][n2] = twiddle48<INV>(q, 2 * n2);      // W_24^{n2}
-    y[2][n2] = twiddle48<INV>(r, 2 * 2 * n2);  // W_24^{2 n2}
+    y[1][n2] = twiddle96<INV>(q, 4 * n2);  // W_24^{n2}
+    y[2][n2] = twiddle96<INV>(r, 8 * n2);  // W_24^{2 n2}
   }
 #pragma unroll
   for (int k1 = 0; k1 < 3; ++k1) {
@@ -144,7 +157,7 @@ __device__ __forceinline__ void dft(float2 (&a)[R]) {
 }
 
 // Values each lane holds for a length-N transform.
-__host__ __device__ constexpr int lane_values(int N) { return N % 3 == 0 ? 24 : 16; }
+__host__ __device__ constexpr int lane_values(int N) { return N % 3 == 0 ? 24 : (N == 512 ? 32 : 16); }
 
 template <int N>
 struct FftShape {
@@ -153,7 +166,7 @@ struct FftShape {
   static constexpr int T = R / G;                    // k1 values per lane after the exchange
   static constexpr int PAD = 1;                      // scratch row padding (bank spread)
   static constexpr int SCR = R * (G + PAD) + 8;      // float2 per group scratch (+8: group offset)
-  static_assert(G >= 2 && G <= 16 && (R % G) == 0 && (G & (G - 1)) == 0, "supported N: 32..256, 192");
+  static_assert(G >= 2 && G <= 16 && (R % G) == 0 && (G & (G - 1)) == 0, "supported N: 32..256, 192, 512");
 };
 
 // Forward FFT of length N over a lane group: v in layout A (natural), out in

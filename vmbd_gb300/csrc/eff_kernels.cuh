@@ -84,10 +84,12 @@ __device__ __forceinline__ void l2_prefetch_bulk(const void* p, unsigned bytes) 
 
 // Half-spectrum bins a CTA stores per row: all N/2+1 (CL = 1) or its
 // quarter plus, on CTA 0, the N/2 bin (CL = 2).
-__host__ __device__ constexpr int frame_pitch(int N, int CL = 1) { return CL == 1 ? N / 2 + 1 : N / 4 + 1; }
+__host__ __device__ constexpr int frame_pitch(int N, int CL = 1) { return CL == 1 ? N / 2 + 1 : N / (2 * CL) + 1; }
 __host__ __device__ constexpr int even_up(int v) { return (v + 1) & ~1; }
 // Threads per CTA the kernel is compiled for (the host may launch fewer).
-__host__ __device__ constexpr int max_threads(int N) { return N % 3 == 0 ? 384 : (N == 256 ? 576 : 512); }
+__host__ __device__ constexpr int max_threads(int N) {
+  return N % 3 == 0 ? 384 : (N == 256 ? 576 : (N == 512 ? 256 : 512));
+}
 
 // Operand A / B of each op, their row counts and frame bases.
 __host__ __device__ constexpr int opnd_a(int op) {
@@ -118,26 +120,25 @@ __device__ __forceinline__ unsigned group_mask(int lane) {
   return G == 32 ? 0xffffffffu : (((1u << G) - 1u) << (lane & ~(G - 1)));
 }
 
-// The half-spectrum frame of one patch, possibly split over a cluster.
+// The half-spectrum frame of one patch, possibly split over a cluster of CL
+// CTAs: CTA c owns the W = N/(2 CL) bins [c W, (c+1) W), CTA 0 also bin N/2
+// (at local column W).
 template <int N, int CL>
 struct Frame {
   static constexpr int HP = frame_pitch(N, CL);
-  static constexpr int Q = N / 4;
+  static constexpr int W = CL == 1 ? N / 2 : N / (2 * CL);
   float2* part[CL];  // generic pointers to every CTA's frame (own one included)
   float2* local;     // this CTA's frame (shared window)
   int rank;
   // Owner and local column of half-spectrum bin b.
-  __device__ __forceinline__ static int owner(int b) { return (CL == 1 || b < Q || b == N / 2) ? 0 : 1; }
+  __device__ __forceinline__ static int owner(int b) { return (CL == 1 || b == N / 2) ? 0 : b / W; }
   __device__ __forceinline__ static int lcol(int b) {
-    return CL == 1 ? b : (b == N / 2 ? Q : (b < Q ? b : b - Q));
+    return CL == 1 ? b : (b == N / 2 ? W : b - (b / W) * W);
   }
   __device__ __forceinline__ float2* at(int row, int b) const {
     return part[owner(b)] + row * HP + lcol(b);
   }
-  // Local columns of column unit u (this CTA owns it): u's bin, and for the
-  // DC unit the N/2 bin.
-  __device__ __forceinline__ int col_of(int u) const { return CL == 1 ? u : u - rank * Q; }
-  static constexpr int kDcN = CL == 1 ? N / 2 : Q;
+  static constexpr int kDcN = W;  // local column of bin N/2 (CTA 0; the DC unit packs it with column 0)
 };
 
 // Window weight ws[k=(m,n)][r][c] from the per-dim (alpha, gamma) tables:
@@ -215,13 +216,18 @@ __device__ __forceinline__ void r2c_store(float2 (&v)[FftShape<N>::R], const Fra
   fft_fwd<N>(v, g, scr, tw, gmask);
   float2 p[R];
   hermitian_partner<N>(v, p, g, gmask);
+  // bins g + G*j of one CTA's range [c W, (c+1) W) are those with j / JW == c
+  // (W is a multiple of G); the N/2 bin (j = R/2, lane 0) goes to CTA 0
+  constexpr int W = Frame<N, CL>::W;
+  constexpr int JW = CL == 1 ? R : R / (2 * CL);
+  static_assert(CL == 1 || (R % (2 * CL)) == 0, "cluster split must align with the lane layout");
 #pragma unroll
   for (int j = 0; j <= R / 2; ++j) {
     if (j == R / 2 && g != 0) break;
     const int kk = g + G * j;
-    // bins g + G*j: j < R/4 (and the N/2 bin, j = R/2) lie in the first quarter
-    float2* base = F.part[(CL == 1 || j < R / 4 || j == R / 2) ? 0 : CL - 1];
-    const int col = CL == 1 ? kk : (j == R / 2 ? Frame<N, CL>::Q : (j < R / 4 ? kk : kk - Frame<N, CL>::Q));
+    const int own = (CL == 1 || j == R / 2) ? 0 : j / JW;
+    float2* base = F.part[own];
+    const int col = CL == 1 ? kk : (j == R / 2 ? W : kk - own * W);
     float2* rowa = base + row * HP + col;
     rowa[0] = make_float2(0.5f * (v[j].x + p[j].x), 0.5f * (v[j].y - p[j].y));
     rowa[HP] = make_float2(0.5f * (v[j].y + p[j].y), 0.5f * (p[j].x - v[j].x));
@@ -543,8 +549,8 @@ __device__ __forceinline__ void eff_patch(const Params& P, int k, long long b, f
     if (tid < 2) {
       const float2* sp = tid == 0 ? b0 : b1;
       if (sp && (reinterpret_cast<unsigned long long>(sp) & 15ull) == 0) {
-        const int c0 = CL == 1 ? 0 : F.rank * (N / 4);
-        const int nc = CL == 1 ? N / 2 + 1 : N / 4;
+        const int c0 = CL == 1 ? 0 : F.rank * Frame<N, CL>::W;
+        const int nc = CL == 1 ? N / 2 + 1 : Frame<N, CL>::W;
         l2_prefetch_bulk(sp + (long long)c0 * N, (unsigned)(nc * N * sizeof(float2)));
         if (CL > 1 && F.rank == 0) l2_prefetch_bulk(sp + (long long)(N / 2) * N, (unsigned)(N * sizeof(float2)));
       }

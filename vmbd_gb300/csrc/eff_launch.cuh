@@ -64,6 +64,7 @@ cudaError_t launch_ncl(int op, const Params& P, int K, int batch, int threads, s
 template <int N>
 cudaError_t launch_n(int op, int CL, const Params& P, int K, int batch, int threads, size_t smem,
                      cudaStream_t st) {
+  if (CL != 1 && CL != 2) return cudaErrorInvalidValue;
   return CL == 2 ? launch_ncl<N, 2>(op, P, K, batch, threads, smem, st)
                  : launch_ncl<N, 1>(op, P, K, batch, threads, smem, st);
 }
@@ -72,5 +73,7 @@ cudaError_t launch_n64(int op, int CL, const Params& P, int K, int batch, int th
 cudaError_t launch_n128(int op, int CL, const Params& P, int K, int batch, int threads, size_t smem, cudaStream_t st);
 cudaError_t launch_n192(int op, int CL, const Params& P, int K, int batch, int threads, size_t smem, cudaStream_t st);
 cudaError_t launch_n256(int op, int CL, const Params& P, int K, int batch, int threads, size_t smem, cudaStream_t st);
+// frame 512: CL = 4 or 8 only
+cudaError_t launch_n512(int op, int CL, const Params& P, int K, int batch, int threads, size_t smem, cudaStream_t st);
 
 }  // namespace eff

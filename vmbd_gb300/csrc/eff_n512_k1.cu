@@ -1,0 +1,8 @@
+// Frame-512 kernels on 4-CTA clusters, ops 0 1 2 (see eff_n512.cu).
+#include "eff_launch.cuh"
+
+namespace eff {
+template cudaError_t launch_one<512, 0, 4>(const Params&, int, int, int, size_t, cudaStream_t);
+template cudaError_t launch_one<512, 1, 4>(const Params&, int, int, int, size_t, cudaStream_t);
+template cudaError_t launch_one<512, 2, 4>(const Params&, int, int, int, size_t, cudaStream_t);
+}  // namespace eff

@@ -127,14 +127,14 @@ def win2winaux(sx, csf, overlap: float = 0.5, windowfun: str = "barthann", sw=No
 
 # Frame edges with compiled kernels; the automatic choice is the smallest
 # power of two that fits (192 is used only when asked for).
-FRAMES = (64, 128, 192, 256)
-AUTO_FRAMES = (64, 128, 256)
+FRAMES = (64, 128, 192, 256, 512)
+AUTO_FRAMES = (64, 128, 256, 512)
 
 
 def fft_frame(sw, sf) -> int:
     """Square frame edge the kernels pick by default: the smallest of 64,
-    128, 256 that is >= sw + sf - 1 in both dims (the linear convolution then
-    fits without wrap-around)."""
+    128, 256, 512 that is >= sw + sf - 1 in both dims (the linear convolution
+    then fits without wrap-around)."""
     e = max(int(sw[0]) + int(sf[0]) - 1, int(sw[1]) + int(sf[1]) - 1)
     for n in AUTO_FRAMES:
         if n >= e:

@@ -165,9 +165,9 @@ class OlaGPU:
             raise NotImplementedError("Not a valid mode!")
         E = [self.winaux.sw[d] + self.sf[d] - 1 for d in range(2)]
         ref = [1 << int(np.ceil(np.log2(e))) for e in E]
-        if ref[0] != ref[1] or ref[0] not in (64, 128, 256):
+        if ref[0] != ref[1] or ref[0] not in (64, 128, 256, 512):
             raise NotImplementedError(f"deconv: the reference frame {ref[0]}x{ref[1]} is not one of the "
-                                      "square frames 64, 128, 256")
+                                      "square frames 64, 128, 256, 512")
         if ref[0] == self.plan.N:
             return self.plan, self.fft_gpu
         if getattr(self, "_dplan", None) is None:
