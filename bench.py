@@ -44,6 +44,12 @@ WORKLOADS = {
                         sx=(512, 512), csf=(8, 8), sf=(31, 31), sw=None, hop=None, kind="motion"),
     "cfg1": dict(desc="256x256, 4x4 grid of 64x64 patches (hop 32), 15x15 Gaussian PSFs, frame 128",
                  sx=(256, 256), csf=(4, 4), sf=(15, 15), sw=(64, 64), hop=(32, 32), kind="gauss"),
+    # the large single-image stress case, literal patches and win2winaux's own geometry
+    "cfg5": dict(desc="2048x2048, 16x16 grid of 192x192 patches (hop 96), 41x41 motion PSFs, frame 256",
+                 sx=(2048, 2048), csf=(16, 16), sf=(41, 41), sw=(192, 192), hop=(96, 96), kind="motion"),
+    "cfg5_winaux": dict(desc="2088x2088 (valid output 2048x2048), 16x16 grid, win2winaux patches 246x246 "
+                             "(hop 123), 41x41 motion PSFs, frame 512",
+                        sx=(2088, 2088), csf=(16, 16), sf=(41, 41), sw=None, hop=None, kind="motion"),
 }
 FLUSH_BYTES = 256 << 20
 # Online multi-frame blind deconvolution: 512x512 frames, 25x25 motion PSFs
