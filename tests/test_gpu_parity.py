@@ -93,8 +93,10 @@ CASES = {
     "cfg1_literal_f192": dict(sx=(256, 256), csf=(4, 4), sf=(15, 15), sw=(64, 64), hop=(32, 32), sfft=192),
     "same_mode": dict(sx=(200, 232), csf=(3, 4), sf=(12, 10), mode="same"),
     "full_mode": dict(sx=(200, 232), csf=(3, 4), sf=(12, 10), mode="full"),
-    # frame 512 (32 values per lane): extent 292 on 4-CTA clusters, 424 on 8-CTA clusters
-    "frame512_cl4": dict(sx=(400, 400), csf=(2, 2), sf=(25, 25), kind="motion"),
+    # frame 512 (32 values per lane): extent 256 < E <= ~270 fits 4-CTA clusters at full
+    # CTA size, larger extents (292, 424) run on 8-CTA clusters
+    "frame512_cl4": dict(sx=(380, 380), csf=(2, 2), sf=(9, 9), sw=(262, 262), hop=(118, 118)),
+    "frame512_cl8a": dict(sx=(400, 400), csf=(2, 2), sf=(25, 25), kind="motion"),
     "frame512_cl8": dict(sx=(600, 600), csf=(2, 2), sf=(25, 25), kind="motion"),
     "frame512_same": dict(sx=(400, 440), csf=(2, 2), sf=(25, 21), mode="same"),
     "full_mode_f192": dict(sx=(200, 232), csf=(3, 4), sf=(12, 10), mode="full", sfft=192),
@@ -102,7 +104,7 @@ CASES = {
 # frame each case runs on
 FRAME = {"cfg1_literal": 128, "cfg1_winaux": 128, "cfg2_literal": 128, "cfg2_winaux": 256,
          "cfg2_winaux_f192": 192, "cfg3_winaux": 256, "cfg3_winaux_f192": 192, "cfg4_mixed": 256,
-         "cfg4_mixed_f192": 192, "cfg1_literal_f192": 192, "frame512_cl4": 512, "frame512_cl8": 512,
+         "cfg4_mixed_f192": 192, "cfg1_literal_f192": 192, "frame512_cl4": 512, "frame512_cl8a": 512, "frame512_cl8": 512,
          "frame512_same": 512}
 
 
@@ -181,7 +183,7 @@ def test_2048_stress_workload(cuda):
 def test_2048_winaux_stress_workload(cuda):
     """The stress image on win2winaux's own geometry: 2088x2088 (valid output
     2048x2048), 16x16 grid of 246x246 patches (hop 123), 41x41 motion PSFs,
-    extent 286: frame 512 on 4-CTA clusters.  Forward against the FP64
+    extent 286: frame 512 on 8-CTA clusters.  Forward against the FP64
     oracle at full size; both adjoints through the adjoint identity."""
     from vmbd_gb300.eff import EffPlan
     wa, g, x, f, r = make(sx=(2088, 2088), csf=(16, 16), sf=(41, 41), kind="motion", seed=23)

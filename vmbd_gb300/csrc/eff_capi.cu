@@ -322,8 +322,9 @@ int eff_plan_create(const EffGeom* geom, const float* win0, const float* win1, E
       p.threads2 = (p.threads2 / 2 + 31) / 32 * 32;
     }
     // Frame 512 runs on clusters of 4 CTAs (each a quarter of the half
-    // spectrum), or of 8 when a quarter frame does not fit; the CTA size is
-    // halved while it does not fit.
+    // spectrum) when a quarter frame fits at the full CTA size, else of 8
+    // (fewer rounds per phase than a 4-CTA cluster of smaller CTAs, for the
+    // same SM time per patch); the 8-CTA size is halved while it does not fit.
     if (p.N == 512) {
       p.clw = 0;
       for (int cl : {4, 8}) {
@@ -335,7 +336,7 @@ int eff_plan_create(const EffGeom* geom, const float* win0, const float* win1, E
             const size_t s = eff::smem_bytes(p.N, op, P, t, cl);
             if (s > worst) worst = s;
           }
-          if (worst <= kSmemLimit || t <= 64) break;
+          if (worst <= kSmemLimit || cl == 4 || t <= 64) break;
           t = (t / 2 + 31) / 32 * 32;
         }
         if (worst <= kSmemLimit) {
