@@ -601,6 +601,19 @@ def cpu_sample(w, wa, x, f, y_obs, r_gpu, budget_s=12.0, max_reps=50, warm=1):
     return statistics.median(times), len(times), cores, out
 
 
+def cpu_sample_single(w, wa, x, f, y_obs, budget_s=4.0, max_reps=10):
+    """The same oracle step with single-threaded numpy.fft (median)."""
+    from oracle import eff64
+    eff64.set_fft_workers(None)
+    times = []
+    t_end = time.perf_counter() + budget_s
+    while len(times) < max_reps and (not times or time.perf_counter() < t_end):
+        t0 = time.perf_counter()
+        oracle_step(w, wa, x, f, y_obs)
+        times.append(time.perf_counter() - t0)
+    return statistics.median(times), len(times)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -729,10 +742,13 @@ def main():
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         r_gpu = R["y"].astype(np.float64) - R["y_obs"]
         t_cpu, reps, cores, (y_o, gx_o, gf_o) = cpu_sample(w, wa, R["x_np"], R["f_np"], R["y_obs"], r_gpu)
+        t1, reps1 = cpu_sample_single(w, wa, R["x_np"], R["f_np"], R["y_obs"])
         line["cpu_baseline"] = {"value": pixels / t_cpu / 1e6, "unit": "Mpixel/s", "cores": cores,
                                 "kind": "port",
                                 "sample": f"{reps} full-image steps of the same workload (FP64 NumPy "
-                                          f"oracle, scipy.fft over {cores} cores), median"}
+                                          f"oracle, scipy.fft over {cores} cores), median",
+                                "single_thread": {"value": pixels / t1 / 1e6, "cores": 1,
+                                                  "sample": f"{reps1} steps, numpy.fft, median"}}
 
         def rel(a, b):
             return float(np.linalg.norm(np.asarray(a, np.float64) - b) / np.linalg.norm(b))
