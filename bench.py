@@ -156,19 +156,29 @@ def run_ours(args, rank, world, dev):
     wa, x_np, f_np = make_inputs(w, seed=rank)
     plan = EffPlan(wa, w["sf"], "valid", device=dev)
     N, K = plan.N, plan.K
-    x = torch.from_numpy(x_np).to(dev)
-    f = torch.from_numpy(f_np).to(dev)
+    # The step's inputs (x, f, y_obs) and outputs (gx, gf, loss) each live in
+    # one device buffer, so that the end-to-end step moves them with one copy
+    # each way (views into the buffers are what the C ABI is given).
+    nx, nf = int(np.prod(plan.sx)), K * int(np.prod(plan.sf))
+    ny = int(np.prod(plan.sy))
+    inbuf = torch.empty(nx + nf + ny, device=dev)
+    x, f = inbuf[:nx].view(plan.sx), inbuf[nx:nx + nf].view((K,) + plan.sf)
+    y_obs = inbuf[nx + nf:].view(plan.sy)
+    x.copy_(torch.from_numpy(x_np))
+    f.copy_(torch.from_numpy(f_np))
     gen = torch.Generator(device=dev).manual_seed(1234 + rank)
-    y_obs = plan.forward_image(x, plan.psf_spectrum(f))
+    y_obs.copy_(plan.forward_image(x, plan.psf_spectrum(f)))
     y_obs += 0.01 * torch.randn(y_obs.shape, device=dev, generator=gen)
 
     # static buffers of the step
     fhat = plan.empty_spectrum()
     xhat = plan.empty_spectrum()
     y = torch.empty(plan.sy, device=dev)
-    gx = torch.empty(plan.sx, device=dev)
-    gf = torch.empty((K,) + plan.sf, device=dev)
-    loss = torch.empty((), dtype=torch.float64, device=dev)
+    o_loss = ((nx + nf) * 4 + 7) // 8 * 8
+    outbuf = torch.empty(o_loss + 8, dtype=torch.uint8, device=dev)
+    gx = outbuf[:nx * 4].view(torch.float32).view(plan.sx)
+    gf = outbuf[nx * 4:(nx + nf) * 4].view(torch.float32).view((K,) + plan.sf)
+    loss = outbuf[o_loss:].view(torch.float64).view(())
 
     def step():
         # fused forward (x, f -> y + both spectra) and fused adjoints of y - y_obs
@@ -276,22 +286,16 @@ def run_ours(args, rank, world, dev):
                 ut += a.elapsed_time(b)
         unfused_ms = ut / args.steps
 
-        # end to end through the public API from pinned host buffers
-        hx = torch.from_numpy(x_np).pin_memory()
-        hf = torch.from_numpy(f_np).pin_memory()
-        hy = y_obs.cpu().pin_memory()
-        ogx = torch.empty(plan.sx).pin_memory()
-        ogf = torch.empty((K,) + plan.sf).pin_memory()
-        oloss = torch.empty((), dtype=torch.float64).pin_memory()
+        # end to end through the public API from pinned host buffers: the
+        # step's inputs in one host->device copy, its outputs in one
+        # device->host copy
+        hin = inbuf.cpu().pin_memory()
+        hout = torch.empty(outbuf.shape, dtype=torch.uint8).pin_memory()
 
         def e2e_step():
-            x.copy_(hx, non_blocking=True)
-            f.copy_(hf, non_blocking=True)
-            y_obs.copy_(hy, non_blocking=True)
+            inbuf.copy_(hin, non_blocking=True)
             graph.replay()
-            ogx.copy_(gx, non_blocking=True)
-            ogf.copy_(gf, non_blocking=True)
-            oloss.copy_(loss, non_blocking=True)
+            hout.copy_(outbuf, non_blocking=True)
 
         for _ in range(args.warmup):
             e2e_step()
@@ -307,8 +311,8 @@ def run_ours(args, rank, world, dev):
             torch.cuda.synchronize(dev)
             et += a.elapsed_time(b)
         et = allreduce_max(et, world, dev)
-    h2d = (hx.numel() + hf.numel() + hy.numel()) * 4
-    d2h = (ogx.numel() + ogf.numel()) * 4 + 8
+    h2d = hin.numel() * 4
+    d2h = hout.numel()
     step()
     k_forward()
     torch.cuda.synchronize(dev)
