@@ -192,16 +192,89 @@ __device__ __forceinline__ float operand(const Params& P, const Patch& T, int r,
   }
 }
 
+// Residual rows (ra, ra+1): which rows and which column range [clo, chi)
+// hold data is worked out once per row pair, so the loads are a straight run
+// of independent reads (OBS: minus y_obs; MSK: times the mask).  Same values
+// as operand<OPND_RESID>.
+template <int N, bool OBS, bool MSK>
+__device__ __forceinline__ void load_resid_rows(const Params& P, const Patch& T, int ra, int g,
+                                                float2 (&v)[FftShape<N>::R]) {
+  constexpr int G = FftShape<N>::G;
+  constexpr int R = FftShape<N>::R;
+  const int i0 = T.m * P.hop0 + ra - P.off0;
+  const bool okA = ra >= P.lo0 && ra < P.hi0 && i0 >= 0 && i0 < P.sy0;
+  const bool okB = ra + 1 >= P.lo0 && ra + 1 < P.hi0 && i0 + 1 >= 0 && i0 + 1 < P.sy0;
+  const int jb = T.n * P.hop1 - P.off1;  // frame column c is image column jb + c
+  const int clo = max(P.lo1, -jb), chi = min(P.hi1, P.sy1 - jb);
+  const long long oa = (long long)i0 * P.sy1 + jb, ob = oa + P.sy1;
+#pragma unroll
+  for (int mm = 0; mm < R; ++mm) {
+    const int c = g + G * mm;
+    const bool cv = c >= clo && c < chi;
+    float a = 0.f, b = 0.f;
+    if (cv && okA) {
+      a = __ldg(T.y + (oa + c));
+      if constexpr (OBS) a -= __ldg(T.y_obs + (oa + c));
+      if constexpr (MSK) a *= __ldg(T.mask + (oa + c));
+    }
+    if (cv && okB) {
+      b = __ldg(T.y + (ob + c));
+      if constexpr (OBS) b -= __ldg(T.y_obs + (ob + c));
+      if constexpr (MSK) b *= __ldg(T.mask + (ob + c));
+    }
+    v[mm] = make_float2(a, b);
+  }
+}
+
+// Windowed image rows (ra, ra+1): the rows' window factors and the valid
+// column range are taken once per row pair.  Same values as
+// operand<OPND_IMAGE>.
+template <int N>
+__device__ __forceinline__ void load_image_rows(const Params& P, const Patch& T, int ra, int g,
+                                                float2 (&v)[FftShape<N>::R]) {
+  constexpr int G = FftShape<N>::G;
+  constexpr int R = FftShape<N>::R;
+  const int i0 = T.m * P.hop0 + ra;
+  const bool okA = ra < P.sw0 && i0 < P.sx0;
+  const bool okB = ra + 1 < P.sw0 && i0 + 1 < P.sx0;
+  const float2 wa = okA ? __ldg(P.win0 + T.m * P.sw0 + ra) : make_float2(0.f, 0.f);
+  const float2 wb = okB ? __ldg(P.win0 + T.m * P.sw0 + ra + 1) : make_float2(0.f, 0.f);
+  const int jb = T.n * P.hop1;
+  const int chi = min(P.sw1, P.sx1 - jb);
+  const long long oa = (long long)i0 * P.sx1 + jb, ob = oa + P.sx1;
+  const float2* w1 = P.win1 + T.n * P.sw1;
+#pragma unroll
+  for (int mm = 0; mm < R; ++mm) {
+    const int c = g + G * mm;
+    float a = 0.f, b = 0.f;
+    if (c < chi) {
+      const float2 wc = __ldg(w1 + c);
+      if (okA) a = window_weight(wa, wc) * __ldg(T.x + (oa + c));
+      if (okB) b = window_weight(wb, wc) * __ldg(T.x + (ob + c));
+    }
+    v[mm] = make_float2(a, b);
+  }
+}
+
 // Operand rows (ra, ra+1) packed as re/im, layout A.
 template <int N, int KIND>
 __device__ __forceinline__ void load_rows(const Params& P, const Patch& T, int ra, int g,
                                           float2 (&v)[FftShape<N>::R]) {
   constexpr int G = FftShape<N>::G;
   constexpr int R = FftShape<N>::R;
+  if constexpr (KIND == OPND_RESID) {
+    if (T.y_obs && !T.mask) load_resid_rows<N, true, false>(P, T, ra, g, v);
+    else if (!T.y_obs && !T.mask) load_resid_rows<N, false, false>(P, T, ra, g, v);
+    else if (!T.y_obs) load_resid_rows<N, false, true>(P, T, ra, g, v);
+    else load_resid_rows<N, true, true>(P, T, ra, g, v);
+  } else if constexpr (KIND == OPND_IMAGE) {
+    load_image_rows<N>(P, T, ra, g, v);
+  } else {
 #pragma unroll
-  for (int mm = 0; mm < R; ++mm) {
-    const int c = g + G * mm;
-    v[mm] = make_float2(operand<KIND>(P, T, ra, c), operand<KIND>(P, T, ra + 1, c));
+    for (int mm = 0; mm < R; ++mm) {
+      const int c = g + G * mm;
+      v[mm] = make_float2(operand<KIND>(P, T, ra, c), operand<KIND>(P, T, ra + 1, c));
+    }
   }
 }
 
