@@ -785,11 +785,25 @@ __device__ __forceinline__ void eff_patch(const Params& P, int k, long long b, f
   if constexpr (OP == OP_ADJ) {
     if (P.loss && T.y_obs) {
       const long long npx = (long long)P.sy0 * P.sy1;
-      const long long chunk = (npx + ncta - 1) / ncta;
-      const long long p0 = (long long)cta * chunk;
+      // shares of whole float4s when both planes are 16-byte aligned
+      const bool vec =
+          ((reinterpret_cast<unsigned long long>(T.y) | reinterpret_cast<unsigned long long>(T.y_obs)) & 15ull) == 0;
+      const long long chunk = vec ? ((npx + ncta - 1) / ncta + 3) & ~3LL : (npx + ncta - 1) / ncta;
+      const long long p0 = min(npx, (long long)cta * chunk);
       const long long p1 = min(npx, p0 + chunk);
+      const long long q1 = vec ? p0 + ((p1 - p0) & ~3LL) : p0;
       float acc = 0.f;
-      for (long long p = p0 + tid; p < p1; p += blockDim.x) {
+      const float4* y4 = reinterpret_cast<const float4*>(T.y + p0);
+      const float4* o4 = reinterpret_cast<const float4*>(T.y_obs + p0);
+      for (int q = tid; q < (int)((q1 - p0) >> 2); q += blockDim.x) {
+        const float4 a = __ldg(y4 + q), o = __ldg(o4 + q);
+        const float r0 = a.x - o.x, r1 = a.y - o.y, r2 = a.z - o.z, r3 = a.w - o.w;
+        acc = fmaf(r0, r0, acc);
+        acc = fmaf(r1, r1, acc);
+        acc = fmaf(r2, r2, acc);
+        acc = fmaf(r3, r3, acc);
+      }
+      for (long long p = q1 + tid; p < p1; p += blockDim.x) {
         const float r = __ldg(T.y + p) - __ldg(T.y_obs + p);
         acc = fmaf(r, r, acc);
       }
