@@ -46,6 +46,7 @@ extern "C" {
 #define EFF_MODE_FULL 2
 
 #define EFF_OUT_ZEROED 1 /* flags: the call's accumulated output is already zero (no memset) */
+#define EFF_LOSS_OF_Y 2  /* eff_adjoint_ex flags: y is already a residual; loss += 0.5 * sum y^2 */
 
 #define EFF_OPERAND_IMAGE 0 /* eff_forward_ex: u is the image, spec the PSF spectrum */
 #define EFF_OPERAND_PSF 1   /* eff_forward_ex: u is the PSF stack, spec the image spectrum */
@@ -119,8 +120,16 @@ int eff_adjoint_residual(const EffPlan* plan, const float* y, const float* y_obs
                          const void* xhat, float* gx, float* gf, double* loss, int adj_mode,
                          int batch, void* stream);
 
-/* One loss/gradient step of 0.5 * ||EFF(x, f) - y_obs||^2: eff_forward_both
- * then eff_adjoint_residual (exact adjoints), with the forward output and
+/* r = EFF(x, f) - y_obs and both spectra (optional) in one kernel:
+ * eff_forward_both whose CTAs also subtract a share each of the observation
+ * (the additions commute with the overlap-add).  An adjoint of r with
+ * EFF_LOSS_OF_Y then reads one plane instead of y and y_obs; eff_loss_grad
+ * is these two kernels.  r must not alias y_obs. */
+int eff_forward_residual(const EffPlan* plan, const float* x, const float* f, const float* y_obs, float* r,
+                         void* xhat_out, void* fhat_out, int batch, void* stream);
+
+/* One loss/gradient step of 0.5 * ||EFF(x, f) - y_obs||^2: eff_forward_residual
+ * then eff_adjoint_ex with EFF_LOSS_OF_Y (exact adjoints), with the residual and
  * the two spectra in a caller-provided device workspace of at least
  * eff_loss_grad_workspace_bytes(plan, batch) bytes.  gx or gf may be NULL
  * (not both); loss may be NULL. */
@@ -199,7 +208,8 @@ int eff_adjoint_masked(const EffPlan* plan, const float* y, const float* mask, c
  *   later call and must not overlap anything this call reads or writes.
  * eff_adjoint_ex: eff_adjoint / eff_adjoint_residual (y_obs) /
  *   eff_adjoint_masked (mask) in one; flags EFF_OUT_ZEROED: gx and loss are
- *   already zero. */
+ *   already zero; EFF_LOSS_OF_Y (no y_obs, no mask): y is the residual, as
+ *   eff_forward_residual leaves it, and loss (nullable) += 0.5 * sum y^2. */
 int eff_forward_ex(const EffPlan* plan, int operand, const float* u, const void* spec, float* y, void* spec_out,
                    int flags, float* zero_f, long long zero_nf, double* zero_d, int zero_nd, int batch,
                    void* stream);

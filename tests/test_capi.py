@@ -72,3 +72,19 @@ def test_compute_entry_points_reject_null_plan():
     assert L.eff_adjoint(None, None, None, None, None, None, 0, 1, None) == _lib.EFF_ERR_INVALID
     assert L.eff_project_psf(None, 1, 1, 0, None) == _lib.EFF_ERR_INVALID
     assert L.eff_spectrum_bytes(None) == 0
+
+
+def test_adjoint_ex_flags_validate_without_gpu():
+    # flag checks run before any CUDA call
+    L = _lib.load()
+    dummy = ctypes.c_void_p(16)
+    assert L.eff_adjoint_ex(None, dummy, dummy, None, dummy, None, dummy, None, dummy, _lib.ADJ_EXACT,
+                            _lib.LOSS_OF_Y, 1, None) == _lib.EFF_ERR_INVALID
+    assert b"LOSS_OF_Y" in L.eff_last_error()
+    assert L.eff_adjoint_ex(None, dummy, None, None, dummy, None, dummy, None, dummy, _lib.ADJ_EXACT,
+                            0, 1, None) == _lib.EFF_ERR_INVALID
+    assert b"y_obs" in L.eff_last_error()
+    assert L.eff_adjoint_ex(None, dummy, None, None, dummy, None, dummy, None, dummy, _lib.ADJ_EXACT,
+                            8, 1, None) == _lib.EFF_ERR_INVALID
+    assert L.eff_forward_residual(None, dummy, dummy, dummy, dummy, None, None, 1, None) == _lib.EFF_ERR_INVALID
+    assert L.eff_forward_residual(None, None, None, None, None, None, None, 1, None) == _lib.EFF_ERR_INVALID

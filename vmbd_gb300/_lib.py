@@ -19,6 +19,7 @@ MODES = {"valid": 0, "same": 1, "full": 2}
 ADJ_EXACT = 0
 ADJ_REFERENCE = 1
 OUT_ZEROED = 1
+LOSS_OF_Y = 2
 OPERAND_IMAGE = 0
 OPERAND_PSF = 1
 PROJ_CLIP_NORMALIZE = 0
@@ -34,7 +35,7 @@ EXPORTS = (
     "eff_adjoint_masked", "eff_dots3", "eff_pg_step", "eff_mu_update", "eff_max_nonneg",
     "eff_set_cluster_mode", "eff_batch_create", "eff_batch_destroy", "eff_batch_items",
     "eff_batch_forward_both", "eff_batch_adjoint_residual", "eff_deconv_xdirect", "eff_forward_ex",
-    "eff_adjoint_ex",
+    "eff_adjoint_ex", "eff_forward_residual",
 )
 
 
@@ -82,6 +83,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "eff_basis_project": ([fp, fp, fp, ip, ip, vp], ip),
         "eff_last_error": ([], ctypes.c_char_p),
         "eff_forward_both": ([vp, fp, fp, fp, vp, vp, ip, vp], ip),
+        "eff_forward_residual": ([vp, fp, fp, fp, fp, vp, vp, ip, vp], ip),
         "eff_adjoint_residual": ([vp, fp, fp, vp, vp, fp, fp, vp, ip, ip, vp], ip),
         "eff_loss_grad_workspace_bytes": ([vp, ip], ctypes.c_size_t),
         "eff_loss_grad": ([vp, fp, fp, fp, vp, fp, fp, vp, ctypes.c_size_t, ip, vp], ip),

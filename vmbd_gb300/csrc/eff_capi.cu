@@ -140,7 +140,7 @@ int check_plan(const EffPlan* p, int batch) {
 // zeroed: gx and loss were already zeroed on the stream (by the fused forward).
 int adjoint_impl(const EffPlan* plan, const float* y, const float* y_obs, const void* fhat,
                  const void* xhat, float* gx, float* gf, double* loss, int adj_mode, int batch,
-                 void* stream, const float* mask = nullptr, bool zeroed = false) {
+                 void* stream, const float* mask = nullptr, bool zeroed = false, bool loss_y = false) {
   if (int s = check_plan(plan, batch)) return s;
   if (!y || (!gx && !gf)) return fail(EFF_ERR_INVALID, "null argument");
   if (gx && !fhat) return fail(EFF_ERR_INVALID, "image adjoint needs the PSF spectrum");
@@ -158,6 +158,7 @@ int adjoint_impl(const EffPlan* plan, const float* y, const float* y_obs, const 
   P.out0 = gx;
   P.out1 = gf;
   P.loss = loss;
+  P.loss_y = loss_y ? 1 : 0;
   P.out0_bs = P.x_bs;
   P.out1_bs = P.f_bs;
   if (adj_mode == EFF_ADJ_REFERENCE) {
@@ -207,7 +208,10 @@ int loss_grad_impl(const EffPlan* plan, const float* x, const float* f, const fl
   float2* xhat = reinterpret_cast<float2*>(ws + w.xhat);
   float2* fhat = reinterpret_cast<float2*>(ws + w.fhat);
   float* y = reinterpret_cast<float*>(ws + w.y);
-  // The fused forward, with the observation prefetched into L2 for the adjoint.
+  // The fused forward accumulates EFF(x, f) - y_obs (each CTA also
+  // subtracts its share of the observation, prefetched into L2 at its
+  // start), so the adjoint reads one plane, the residual, and takes the loss
+  // from it.
   eff::Params P = base_params(plan);
   P.x = x;
   P.f = f;
@@ -217,6 +221,7 @@ int loss_grad_impl(const EffPlan* plan, const float* x, const float* f, const fl
   P.b_out = gx ? fhat : nullptr;
   P.pf = reinterpret_cast<const char*>(y_obs);
   P.pf_bytes = (long long)sizeof(float) * P.y_bs;
+  P.sub = y_obs;
   // the forward also zeroes the adjoint's accumulators (no memset nodes)
   P.zero_f = gx;
   P.zero_nf = gx ? P.x_bs * batch : 0;
@@ -226,8 +231,8 @@ int loss_grad_impl(const EffPlan* plan, const float* x, const float* f, const fl
   if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
   int s = run(plan, eff::OP_FWD_BOTH, P, batch, stream);
   if (s != EFF_OK) return s;
-  return adjoint_impl(plan, y, y_obs, gx ? fhat : nullptr, gf ? xhat : nullptr, gx, gf, loss,
-                      EFF_ADJ_EXACT, batch, stream, nullptr, true);
+  return adjoint_impl(plan, y, nullptr, gx ? fhat : nullptr, gf ? xhat : nullptr, gx, gf, loss,
+                      EFF_ADJ_EXACT, batch, stream, nullptr, true, true);
 }
 
 }  // namespace
@@ -501,10 +506,12 @@ int eff_forward_ex(const EffPlan* plan, int operand, const float* u, const void*
 int eff_adjoint_ex(const EffPlan* plan, const float* y, const float* y_obs, const float* mask, const void* fhat,
                    const void* xhat, float* gx, float* gf, double* loss, int adj_mode, int flags, int batch,
                    void* stream) {
-  if (flags & ~EFF_OUT_ZEROED) return fail(EFF_ERR_INVALID, "flags");
-  if (loss && !y_obs) return fail(EFF_ERR_INVALID, "the loss needs y_obs");
+  if (flags & ~(EFF_OUT_ZEROED | EFF_LOSS_OF_Y)) return fail(EFF_ERR_INVALID, "flags");
+  const bool loss_y = (flags & EFF_LOSS_OF_Y) != 0;
+  if (loss_y && (y_obs || mask)) return fail(EFF_ERR_INVALID, "EFF_LOSS_OF_Y takes no y_obs or mask");
+  if (loss && !y_obs && !loss_y) return fail(EFF_ERR_INVALID, "the loss needs y_obs (or EFF_LOSS_OF_Y)");
   return adjoint_impl(plan, y, y_obs, fhat, xhat, gx, gf, loss, adj_mode, batch, stream, mask,
-                      (flags & EFF_OUT_ZEROED) != 0);
+                      (flags & EFF_OUT_ZEROED) != 0, loss_y);
 }
 
 int eff_adjoint(const EffPlan* plan, const float* y, const void* fhat, const void* xhat, float* gx,
@@ -566,6 +573,26 @@ int eff_forward_both(const EffPlan* plan, const float* x, const float* f, float*
   P.a_out = static_cast<float2*>(xhat_out);
   P.b_out = static_cast<float2*>(fhat_out);
   cudaError_t e = cudaMemsetAsync(y, 0, sizeof(float) * P.y_bs * batch, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+  return run(plan, eff::OP_FWD_BOTH, P, batch, stream);
+}
+
+int eff_forward_residual(const EffPlan* plan, const float* x, const float* f, const float* y_obs, float* r,
+                         void* xhat_out, void* fhat_out, int batch, void* stream) {
+  if (int s = check_plan(plan, batch)) return s;
+  if (!x || !f || !y_obs || !r) return fail(EFF_ERR_INVALID, "null argument");
+  if (r == y_obs) return fail(EFF_ERR_INVALID, "r must not alias y_obs");
+  eff::Params P = base_params(plan);
+  P.x = x;
+  P.f = f;
+  P.out0 = r;
+  P.out0_bs = P.y_bs;
+  P.a_out = static_cast<float2*>(xhat_out);
+  P.b_out = static_cast<float2*>(fhat_out);
+  P.pf = reinterpret_cast<const char*>(y_obs);
+  P.pf_bytes = (long long)sizeof(float) * P.y_bs;
+  P.sub = y_obs;
+  cudaError_t e = cudaMemsetAsync(r, 0, sizeof(float) * P.y_bs * batch, static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
   return run(plan, eff::OP_FWD_BOTH, P, batch, stream);
 }

@@ -74,6 +74,9 @@ struct Params {
   long long zero_nf;       //   accumulator), spread over the grid
   double* zero_d;          // eff_kernel: zero [zero_d, zero_d + zero_nd)
   int zero_nd;
+  const float* sub;        // forward: subtract this plane [sy0, sy1] from out0 too (a share per CTA, by
+                           //   atomics), so that out0 ends as EFF(...) - sub
+  int loss_y;              // adjoint without y_obs: loss += 0.5 * sum y^2 (y is already the residual)
 };
 
 // TMA bulk prefetch of a contiguous range into L2 (16-byte aligned start and
@@ -734,6 +737,25 @@ __device__ __forceinline__ void eff_patch(const Params& P, int k, long long b, f
         }
       }
     }
+    // out -= sub over this CTA's share of the pixels: the additions commute
+    // with the other CTAs' overlap-add, so out ends as the residual
+    if (P.sub) {
+      const float* sb = P.sub + b * P.y_bs;
+      const long long npx = (long long)P.sy0 * P.sy1;
+      const bool vec = ((reinterpret_cast<unsigned long long>(out) | reinterpret_cast<unsigned long long>(sb)) &
+                        15ull) == 0;
+      const long long chunk = vec ? ((npx + ncta - 1) / ncta + 3) & ~3LL : (npx + ncta - 1) / ncta;
+      const long long p0 = min(npx, (long long)cta * chunk);
+      const long long p1 = min(npx, p0 + chunk);
+      const long long q1 = vec ? p0 + ((p1 - p0) & ~3LL) : p0;
+      const float4* s4 = reinterpret_cast<const float4*>(sb + p0);
+      float4* o4 = reinterpret_cast<float4*>(out + p0);
+      for (int q = tid; q < (int)((q1 - p0) >> 2); q += blockDim.x) {
+        const float4 s = __ldg(s4 + q);
+        atomicAdd(o4 + q, make_float4(-s.x, -s.y, -s.z, -s.w));
+      }
+      for (long long p = q1 + tid; p < p1; p += blockDim.x) atomicAdd(out + p, -__ldg(sb + p));
+    }
   } else if constexpr (OP == OP_ADJ || OP == OP_DECONV) {
     const int n0 = P.out0 ? (P.sw0 + 1) >> 1 : 0;
     const int n1 = P.out1 ? (P.sf0 + 1) >> 1 : 0;
@@ -783,7 +805,7 @@ __device__ __forceinline__ void eff_patch(const Params& P, int k, long long b, f
   // Loss of the residual: this CTA's contiguous share of the pixels (after
   // the transforms, when the observation is in L2).
   if constexpr (OP == OP_ADJ) {
-    if (P.loss && T.y_obs) {
+    if (P.loss && (T.y_obs || P.loss_y)) {
       const long long npx = (long long)P.sy0 * P.sy1;
       // shares of whole float4s when both planes are 16-byte aligned
       const bool vec =
@@ -795,17 +817,31 @@ __device__ __forceinline__ void eff_patch(const Params& P, int k, long long b, f
       float acc = 0.f;
       const float4* y4 = reinterpret_cast<const float4*>(T.y + p0);
       const float4* o4 = reinterpret_cast<const float4*>(T.y_obs + p0);
-      for (int q = tid; q < (int)((q1 - p0) >> 2); q += blockDim.x) {
-        const float4 a = __ldg(y4 + q), o = __ldg(o4 + q);
-        const float r0 = a.x - o.x, r1 = a.y - o.y, r2 = a.z - o.z, r3 = a.w - o.w;
-        acc = fmaf(r0, r0, acc);
-        acc = fmaf(r1, r1, acc);
-        acc = fmaf(r2, r2, acc);
-        acc = fmaf(r3, r3, acc);
-      }
-      for (long long p = q1 + tid; p < p1; p += blockDim.x) {
-        const float r = __ldg(T.y + p) - __ldg(T.y_obs + p);
-        acc = fmaf(r, r, acc);
+      if (T.y_obs) {
+        for (int q = tid; q < (int)((q1 - p0) >> 2); q += blockDim.x) {
+          const float4 a = __ldg(y4 + q), o = __ldg(o4 + q);
+          const float r0 = a.x - o.x, r1 = a.y - o.y, r2 = a.z - o.z, r3 = a.w - o.w;
+          acc = fmaf(r0, r0, acc);
+          acc = fmaf(r1, r1, acc);
+          acc = fmaf(r2, r2, acc);
+          acc = fmaf(r3, r3, acc);
+        }
+        for (long long p = q1 + tid; p < p1; p += blockDim.x) {
+          const float r = __ldg(T.y + p) - __ldg(T.y_obs + p);
+          acc = fmaf(r, r, acc);
+        }
+      } else {
+        for (int q = tid; q < (int)((q1 - p0) >> 2); q += blockDim.x) {
+          const float4 a = __ldg(y4 + q);
+          acc = fmaf(a.x, a.x, acc);
+          acc = fmaf(a.y, a.y, acc);
+          acc = fmaf(a.z, a.z, acc);
+          acc = fmaf(a.w, a.w, acc);
+        }
+        for (long long p = q1 + tid; p < p1; p += blockDim.x) {
+          const float r = __ldg(T.y + p);
+          acc = fmaf(r, r, acc);
+        }
       }
       double d = acc;
 #pragma unroll

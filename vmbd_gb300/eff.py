@@ -146,9 +146,11 @@ class EffPlan:
                                             b or 1, _stream(self.device)))
         return out
 
-    def forward_both(self, x, f, out=None, xhat_out=None, fhat_out=None):
+    def forward_both(self, x, f, out=None, xhat_out=None, fhat_out=None, subtract=None):
         """y = EFF(x, f) from raw image and PSFs in one kernel; optionally
-        leaves both spectra behind for a later ``adjoint``."""
+        leaves both spectra behind for a later ``adjoint``.  ``subtract``
+        (an observation y_obs): returns the residual EFF(x, f) - y_obs,
+        formed by the same kernel."""
         x, b = self._check(x, self.sx, "x")
         f, bf = self._check(f, (self.K,) + self.sf, "f")
         if bf != b:
@@ -158,6 +160,14 @@ class EffPlan:
                 self._check_spec(s_, b, n)
         if out is None:
             out = torch.empty(((b,) if b else ()) + self.sy, dtype=torch.float32, device=self.device)
+        if subtract is not None:
+            subtract, bs = self._check(subtract, self.sy, "subtract")
+            if bs != b:
+                raise IOError("Size missmatch: x and subtract batch dims differ")
+            _lib.check(self.lib.eff_forward_residual(self._h, _ptr(x), _ptr(f), _ptr(subtract), _ptr(out),
+                                                     _ptr(xhat_out), _ptr(fhat_out), b or 1,
+                                                     _stream(self.device)))
+            return out
         _lib.check(self.lib.eff_forward_both(self._h, _ptr(x), _ptr(f), _ptr(out), _ptr(xhat_out),
                                              _ptr(fhat_out), b or 1, _stream(self.device)))
         return out
@@ -202,12 +212,14 @@ class EffPlan:
                             loss=loss, want_loss=want_loss)
 
     def adjoint(self, y, fhat=None, xhat=None, want_image=True, want_psf=True,
-                adjoint="exact", gx=None, gf=None, y_obs=None, loss=None, want_loss=True):
+                adjoint="exact", gx=None, gf=None, y_obs=None, loss=None, want_loss=True, residual=False):
         """F.cnvtp(y) and/or X.cnvtp(y) from one transform of y.
 
         Returns ``(gx, gf)``; an output that is not wanted is None.
         ``adjoint``: 'exact' (transpose of the forward) or 'reference'
-        (OlaGPU.cnvtp's truncated chop)."""
+        (OlaGPU.cnvtp's truncated chop).  ``residual=True``: y is already a
+        residual (``forward_both(..., subtract=y_obs)``); returns
+        ``(loss, gx, gf)`` with loss = 0.5 * ||y||^2 (float64)."""
         if adjoint not in ("exact", "reference"):
             raise ValueError("adjoint must be 'exact' or 'reference'")
         if adjoint == "reference" and self.mode not in ("valid", "same"):
@@ -231,6 +243,17 @@ class EffPlan:
         else:
             gf = None
         mode = _lib.ADJ_EXACT if adjoint == "exact" else _lib.ADJ_REFERENCE
+        if residual:
+            if y_obs is not None:
+                raise ValueError("residual=True takes no y_obs")
+            if not want_loss:
+                loss = None
+            elif loss is None:
+                loss = torch.empty(lead, dtype=torch.float64, device=self.device)
+            _lib.check(self.lib.eff_adjoint_ex(self._h, _ptr(y), None, None, _ptr(fhat if want_image else None),
+                                               _ptr(xhat if want_psf else None), _ptr(gx), _ptr(gf), _ptr(loss),
+                                               mode, _lib.LOSS_OF_Y, b or 1, _stream(self.device)))
+            return loss, gx, gf
         if y_obs is None:
             _lib.check(self.lib.eff_adjoint(self._h, _ptr(y), _ptr(fhat if want_image else None),
                                             _ptr(xhat if want_psf else None), _ptr(gx), _ptr(gf), mode,
