@@ -202,7 +202,10 @@ int eff_adjoint_masked(const EffPlan* plan, const float* y, const float* mask, c
  * let each accumulated output be zeroed as a side job of an earlier kernel
  * that does not touch it, and its own call skip the memset.
  * eff_forward_ex: eff_forward_image (operand EFF_OPERAND_IMAGE, spec =
- *   fhat) or eff_forward_psf (EFF_OPERAND_PSF, spec = xhat); flags
+ *   fhat) or eff_forward_psf (EFF_OPERAND_PSF, spec = xhat); sub
+ *   (nullable, not aliasing y): y = EFF - sub, the residual against an
+ *   observation sub, formed by the same kernel as in eff_forward_residual;
+ *   flags
  *   EFF_OUT_ZEROED: y is already zero; zero_f[0, zero_nf) (float) and
  *   zero_d[0, zero_nd) (double), nullable, are cleared by the kernel for a
  *   later call and must not overlap anything this call reads or writes.
@@ -210,9 +213,9 @@ int eff_adjoint_masked(const EffPlan* plan, const float* y, const float* mask, c
  *   eff_adjoint_masked (mask) in one; flags EFF_OUT_ZEROED: gx and loss are
  *   already zero; EFF_LOSS_OF_Y (no y_obs, no mask): y is the residual, as
  *   eff_forward_residual leaves it, and loss (nullable) += 0.5 * sum y^2. */
-int eff_forward_ex(const EffPlan* plan, int operand, const float* u, const void* spec, float* y, void* spec_out,
-                   int flags, float* zero_f, long long zero_nf, double* zero_d, int zero_nd, int batch,
-                   void* stream);
+int eff_forward_ex(const EffPlan* plan, int operand, const float* u, const void* spec, float* y, const float* sub,
+                   void* spec_out, int flags, float* zero_f, long long zero_nf, double* zero_d, int zero_nd,
+                   int batch, void* stream);
 int eff_adjoint_ex(const EffPlan* plan, const float* y, const float* y_obs, const float* mask, const void* fhat,
                    const void* xhat, float* gx, float* gf, double* loss, int adj_mode, int flags, int batch,
                    void* stream);
@@ -263,8 +266,13 @@ int eff_batch_items(const EffBatch* batch);
 /* eff_forward_both over the batch: x, f -> y (+ both spectra, nullable). */
 int eff_batch_forward_both(const EffBatch* batch, const float* const* x, const float* const* f, float* const* y,
                            void* const* xhat_out, void* const* fhat_out, void* stream);
-/* eff_adjoint_residual over the batch (y_obs and loss nullable: plain
- * adjoint of y); gx needs fhat, gf needs xhat. */
+/* eff_forward_residual over the batch: r = EFF(x, f) - y_obs per image. */
+int eff_batch_forward_residual(const EffBatch* batch, const float* const* x, const float* const* f,
+                               const float* const* y_obs, float* const* r, void* const* xhat_out,
+                               void* const* fhat_out, void* stream);
+/* eff_adjoint_residual over the batch; y_obs nullable: y is already the
+ * residual (eff_batch_forward_residual) and loss (nullable) = 0.5 * sum y^2;
+ * gx needs fhat, gf needs xhat. */
 int eff_batch_adjoint_residual(const EffBatch* batch, const float* const* y, const float* const* y_obs,
                                const void* const* fhat, const void* const* xhat, float* const* gx,
                                float* const* gf, double* const* loss, void* stream);

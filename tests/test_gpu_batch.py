@@ -48,8 +48,20 @@ def test_persistent_batch_matches_single_launches(cuda, specs, counts):
     B = EffBatch(plans, counts)
     assert B.items == sum(p.K * c for p, c in zip(plans, counts))
     xs, fs, yo = [c[1] for c in cls], [c[2] for c in cls], [c[3] for c in cls]
-    ys = B.forward_both(xs, fs)
+    xhs = [p.empty_spectrum(c) for p, c in zip(plans, counts)]
+    fhs = [p.empty_spectrum(c) for p, c in zip(plans, counts)]
+    ys = B.forward_both(xs, fs, xhats=xhs, fhats=fhs)
     losses, gxs, gfs = B.loss_grad(xs, fs, yo)
+    # the adjoint of y - y_obs formed in its row loads, and the residual
+    # forward; the residual is noise-sized (1e-2 of y), so FP32 rounding of y
+    # (~1e-7) is ~1e-5 of it
+    l2s, gx2s, gf2s = B.adjoint_residual(ys, yo, fhs, xhs)
+    rs = B.forward_both(xs, fs, subtracts=yo)
+    for i in range(len(cls)):
+        assert rel(rs[i].cpu(), (ys[i] - yo[i]).cpu()) < 1e-4
+        assert rel(gx2s[i].cpu(), gxs[i].cpu()) < 1e-4
+        assert rel(gf2s[i].cpu(), gfs[i].cpu()) < 1e-4
+        assert rel(l2s[i].cpu(), losses[i].cpu()) < 1e-4
     for i, (plan, x, f, y_obs) in enumerate(cls):
         y1 = plan.forward_both(x, f)
         assert rel(ys[i].cpu(), y1.cpu()) < 1e-6

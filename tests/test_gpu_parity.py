@@ -434,10 +434,15 @@ def test_chained_call_entry_points(cuda):
             y = torch.zeros_like(want) if flags else torch.full_like(want, 7.0)
             side_f = torch.ones(12345, device=cuda)
             side_d = torch.ones(3, dtype=torch.float64, device=cuda)
-            _lib.check(L.eff_forward_ex(plan._h, operand, _ptr(u), _ptr(spec), _ptr(y), None, flags, _ptr(side_f),
-                                        side_f.numel(), _ptr(side_d), 3, 1, st))
+            _lib.check(L.eff_forward_ex(plan._h, operand, _ptr(u), _ptr(spec), _ptr(y), None, None, flags,
+                                        _ptr(side_f), side_f.numel(), _ptr(side_d), 3, 1, st))
             assert rel(y.cpu(), want.cpu()) < 1e-6
             assert not side_f.any() and not side_d.any()
+            # residual against an observation, formed by the same kernel
+            res = torch.zeros_like(want) if flags else torch.full_like(want, 7.0)
+            _lib.check(L.eff_forward_ex(plan._h, operand, _ptr(u), _ptr(spec), _ptr(res), _ptr(rt), None, flags,
+                                        None, 0, None, 0, 1, st))
+            assert rel(res.cpu(), (want - rt).cpu()) < 1e-6
     mask = (torch.rand(plan.sy, device=cuda, generator=torch.Generator(device=cuda).manual_seed(3)) > 0.3).float()
     gx_ref, _ = plan.adjoint(rt * mask, fh, xh, want_psf=False)
     yo = 0.5 * rt
@@ -454,7 +459,9 @@ def test_chained_call_entry_points(cuda):
                                     _ptr(loss), _lib.ADJ_EXACT, flags, 1, st))
         assert rel(gf.cpu(), gf_ref.cpu()) < 1e-6
         assert abs(float(loss) - float(loss_ref)) < 1e-6 * float(loss_ref)
-    assert L.eff_forward_ex(plan._h, 5, _ptr(xt), _ptr(fh), _ptr(y_img), None, 0, None, 0, None, 0, 1, st) \
+    assert L.eff_forward_ex(plan._h, 5, _ptr(xt), _ptr(fh), _ptr(y_img), None, None, 0, None, 0, None, 0, 1, st) \
         == _lib.EFF_ERR_INVALID
+    assert L.eff_forward_ex(plan._h, _lib.OPERAND_IMAGE, _ptr(xt), _ptr(fh), _ptr(y_img), _ptr(y_img), None, 0,
+                            None, 0, None, 0, 1, st) == _lib.EFF_ERR_INVALID
     assert L.eff_adjoint_ex(plan._h, _ptr(rt), None, None, _ptr(fh), None, _ptr(gx_ref), None, None,
                             _lib.ADJ_EXACT, 4, 1, st) == _lib.EFF_ERR_INVALID

@@ -35,7 +35,7 @@ EXPORTS = (
     "eff_adjoint_masked", "eff_dots3", "eff_pg_step", "eff_mu_update", "eff_max_nonneg",
     "eff_set_cluster_mode", "eff_batch_create", "eff_batch_destroy", "eff_batch_items",
     "eff_batch_forward_both", "eff_batch_adjoint_residual", "eff_deconv_xdirect", "eff_forward_ex",
-    "eff_adjoint_ex", "eff_forward_residual",
+    "eff_adjoint_ex", "eff_forward_residual", "eff_batch_forward_residual",
 )
 
 
@@ -98,10 +98,11 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "eff_batch_destroy": ([vp], ip),
         "eff_batch_items": ([vp], ip),
         "eff_batch_forward_both": ([vp, vp, vp, vp, vp, vp, vp], ip),
+        "eff_batch_forward_residual": ([vp, vp, vp, vp, vp, vp, vp, vp], ip),
         "eff_batch_adjoint_residual": ([vp, vp, vp, vp, vp, vp, vp, vp, vp], ip),
         "eff_mu_update": ([fp, fp, fp, ctypes.c_float, ip, ip, ip, ip, vp, ctypes.c_float, vp, ip, fp,
                            ctypes.c_longlong, vp], ip),
-        "eff_forward_ex": ([vp, ip, fp, vp, fp, vp, ip, fp, ctypes.c_longlong, vp, ip, ip, vp], ip),
+        "eff_forward_ex": ([vp, ip, fp, vp, fp, fp, vp, ip, fp, ctypes.c_longlong, vp, ip, ip, vp], ip),
         "eff_adjoint_ex": ([vp, fp, fp, fp, vp, vp, fp, fp, vp, ip, ip, ip, vp], ip),
         "eff_loss_grad_static": ([vp, fp, fp, fp, vp, fp, fp, ip, vp], ip),
         "eff_deconv_xdirect": ([vp, fp, vp, vp, fp, fp, ctypes.c_float, ctypes.c_float, ip, vp], ip),

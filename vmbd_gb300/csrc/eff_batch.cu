@@ -192,6 +192,10 @@ int batch_run(const EffBatch* B, int op, const float* const* x, const float* con
       P.out0_bs = P.y_bs;
       P.a_out = a_out ? static_cast<float2*>(a_out[c]) : nullptr;
       P.b_out = b_out ? static_cast<float2*>(b_out[c]) : nullptr;
+      if (y_obs) {  // residual forward: the output ends as EFF - y_obs
+        if (!y_obs[c] || y_obs[c] == y[c]) return set_error(EFF_ERR_INVALID, "bad y_obs");
+        P.sub = y_obs[c];
+      }
       cudaError_t e = cudaMemsetAsync(P.out0, 0, sizeof(float) * P.y_bs * batch, st);
       if (e != cudaSuccess) return set_error(EFF_ERR_CUDA, std::string("memset: ") + cudaGetErrorString(e));
     } else {
@@ -202,7 +206,8 @@ int batch_run(const EffBatch* B, int op, const float* const* x, const float* con
       P.b1 = spec1 ? static_cast<const float2*>(spec1[c]) : nullptr;
       P.out0 = out0 ? out0[c] : nullptr;
       P.out1 = out1 ? out1[c] : nullptr;
-      P.loss = (loss && P.y_obs) ? loss[c] : nullptr;
+      P.loss = loss ? loss[c] : nullptr;
+      P.loss_y = P.y_obs ? 0 : 1;  // no y_obs: y is the residual
       P.out0_bs = P.x_bs;
       P.out1_bs = P.f_bs;
       if (!P.out0 && !P.out1) return set_error(EFF_ERR_INVALID, "no adjoint output");
@@ -230,6 +235,14 @@ extern "C" {
 int eff_batch_forward_both(const EffBatch* batch, const float* const* x, const float* const* f, float* const* y,
                            void* const* xhat_out, void* const* fhat_out, void* stream) {
   return eff::batch_run(batch, eff::OP_FWD_BOTH, x, f, y, nullptr, nullptr, nullptr, nullptr, nullptr, xhat_out,
+                        fhat_out, nullptr, stream);
+}
+
+int eff_batch_forward_residual(const EffBatch* batch, const float* const* x, const float* const* f,
+                               const float* const* y_obs, float* const* r, void* const* xhat_out,
+                               void* const* fhat_out, void* stream) {
+  if (!y_obs) return eff::set_error(EFF_ERR_INVALID, "null y_obs");
+  return eff::batch_run(batch, eff::OP_FWD_BOTH, x, f, r, y_obs, nullptr, nullptr, nullptr, nullptr, xhat_out,
                         fhat_out, nullptr, stream);
 }
 

@@ -477,11 +477,12 @@ int eff_forward_psf(const EffPlan* plan, const float* f, const void* xhat, float
   return run(plan, eff::OP_FWD_PSF, P, batch, stream);
 }
 
-int eff_forward_ex(const EffPlan* plan, int operand, const float* u, const void* spec, float* y, void* spec_out,
-                   int flags, float* zero_f, long long zero_nf, double* zero_d, int zero_nd, int batch,
-                   void* stream) {
+int eff_forward_ex(const EffPlan* plan, int operand, const float* u, const void* spec, float* y, const float* sub,
+                   void* spec_out, int flags, float* zero_f, long long zero_nf, double* zero_d, int zero_nd,
+                   int batch, void* stream) {
   if (int s = check_plan(plan, batch)) return s;
   if (!u || !spec || !y) return fail(EFF_ERR_INVALID, "null argument");
+  if (sub == y) return fail(EFF_ERR_INVALID, "sub must not alias y");
   if (operand != EFF_OPERAND_IMAGE && operand != EFF_OPERAND_PSF) return fail(EFF_ERR_INVALID, "operand");
   if ((flags & ~EFF_OUT_ZEROED) || zero_nf < 0 || zero_nd < 0 || (zero_nf > 0 && !zero_f) || (zero_nd > 0 && !zero_d))
     return fail(EFF_ERR_INVALID, "bad argument");
@@ -491,6 +492,7 @@ int eff_forward_ex(const EffPlan* plan, int operand, const float* u, const void*
   P.b0 = static_cast<const float2*>(spec);
   P.out0 = y;
   P.out0_bs = P.y_bs;
+  P.sub = sub;
   P.a_out = static_cast<float2*>(spec_out);
   P.zero_f = zero_nf > 0 ? zero_f : nullptr;
   P.zero_nf = zero_nf;

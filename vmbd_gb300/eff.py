@@ -373,16 +373,26 @@ class EffBatch:
             if tuple(t.shape) != want or t.dtype != torch.float32 or not t.is_contiguous() or not t.is_cuda:
                 raise IOError(f"{name}: expected contiguous float32 CUDA tensor {want}, got {tuple(t.shape)}")
 
-    def forward_both(self, xs, fs, ys=None, xhats=None, fhats=None):
+    def forward_both(self, xs, fs, ys=None, xhats=None, fhats=None, subtracts=None):
+        """Per image y = EFF(x, f); with ``subtracts`` (observations) the
+        residuals EFF(x, f) - y_obs instead."""
         self._shapes(xs, lambda p: p.sx, "x")
         self._shapes(fs, lambda p: (p.K,) + p.sf, "f")
         if ys is None:
             ys = [torch.empty((c,) + p.sy, device=self.device) for p, c in zip(self.plans, self.counts)]
+        if subtracts is not None:
+            self._shapes(subtracts, lambda p: p.sy, "subtract")
+            _lib.check(self.lib.eff_batch_forward_residual(
+                self._h, self._ptrs(xs), self._ptrs(fs), self._ptrs(subtracts), self._ptrs(ys),
+                self._ptrs(xhats), self._ptrs(fhats), _stream(self.device)))
+            return ys
         _lib.check(self.lib.eff_batch_forward_both(self._h, self._ptrs(xs), self._ptrs(fs), self._ptrs(ys),
                                                    self._ptrs(xhats), self._ptrs(fhats), _stream(self.device)))
         return ys
 
     def adjoint_residual(self, ys, y_obss, fhats, xhats, gxs=None, gfs=None, losses=None):
+        """Per image the adjoints of y - y_obs and 0.5 * ||y - y_obs||^2;
+        ``y_obss`` None: each y is already a residual."""
         if gxs is None:
             gxs = [torch.empty((c,) + p.sx, device=self.device) for p, c in zip(self.plans, self.counts)]
         if gfs is None:
@@ -400,9 +410,9 @@ class EffBatch:
             self._work = ([torch.empty((c,) + p.sy, device=self.device) for p, c in zip(self.plans, self.counts)],
                           [p.empty_spectrum(c) for p, c in zip(self.plans, self.counts)],
                           [p.empty_spectrum(c) for p, c in zip(self.plans, self.counts)])
-        ys, xh, fh = self._work
-        self.forward_both(xs, fs, ys, xh, fh)
-        return self.adjoint_residual(ys, y_obss, fh, xh, gxs, gfs, losses)
+        rs, xh, fh = self._work
+        self.forward_both(xs, fs, rs, xh, fh, subtracts=y_obss)
+        return self.adjoint_residual(rs, None, fh, xh, gxs, gfs, losses)
 
 
 def set_cluster_mode(mode: int) -> None:

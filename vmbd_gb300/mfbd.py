@@ -109,17 +109,17 @@ class OnlineMFBD:
         # --- PSF estimation: X object of the current latent image --------
         P.image_spectrum(self.x, out=self.xhat)
         for k in range(self.n_pg):
-            # y_pred = X f (y_pred cleared by the previous PSF step; memset at
-            # k = 0); side jobs: clear dots (and yg at k = 0)
+            # residual X f - y into y_pred (cleared by the previous PSF step;
+            # memset at k = 0); side jobs: clear dots (and yg at k = 0)
             self._check(L.eff_forward_ex(P._h, _lib.OPERAND_PSF, _ptr(self.f), _ptr(self.xhat), _ptr(self.ypred),
-                                         None, OZ if k > 0 else 0, _ptr(self.yg) if k == 0 else None,
+                                         _ptr(self.y), None, OZ if k > 0 else 0, _ptr(self.yg) if k == 0 else None,
                                          ny if k == 0 else 0, _ptr(self.dots), 3, 1, st))
-            # g = X^T (y_pred - y); the BB / exact-line-search steps need no objective value
-            self._check(L.eff_adjoint_ex(P._h, _ptr(self.ypred), _ptr(self.y), None, None, _ptr(self.xhat),
+            # g = X^T (X f - y); the BB / exact-line-search steps need no objective value
+            self._check(L.eff_adjoint_ex(P._h, _ptr(self.ypred), None, None, None, _ptr(self.xhat),
                                          None, _ptr(self.g), None, amode, 0, 1, st))
             if k == 0:
                 self._check(L.eff_forward_ex(P._h, _lib.OPERAND_PSF, _ptr(self.g), _ptr(self.xhat),
-                                             _ptr(self.yg), None, OZ, None, 0, None, 0, 1, st))
+                                             _ptr(self.yg), None, None, OZ, None, 0, None, 0, 1, st))
                 self._check(L.eff_dots3(_ptr(self.g), None, K * n, _ptr(self.yg), None, ny,
                                         _ptr(self.dots), OZ, st))
                 mode = 0
@@ -139,7 +139,7 @@ class OnlineMFBD:
             # y_pred = F x (y_pred cleared by the previous PSF step or image
             # step); side job: clear den and the interior-maximum word
             self._check(L.eff_forward_ex(P._h, _lib.OPERAND_IMAGE, _ptr(self.x), _ptr(self.fhat),
-                                         _ptr(self.ypred), None, OZ if (i > 0 or self.n_pg > 0) else 0,
+                                         _ptr(self.ypred), None, None, OZ if (i > 0 or self.n_pg > 0) else 0,
                                          _ptr(self._denx), nx + 1, None, 0, 1, st))
             self._check(L.eff_adjoint_ex(P._h, _ptr(self.ypred), None, _ptr(self.mask), _ptr(self.fhat), None,
                                          _ptr(self.den), None, None, amode, OZ, 1, st))
