@@ -486,64 +486,31 @@ __device__ __forceinline__ void column_divide(const float2 (&a)[FftShape<N>::R],
   }
 }
 
-// OP_FWD_BOTH, column unit 0: columns 0 and N/2 of both operands are real.
-// Column 0 of the image and column 0 of the PSFs share one complex transform
-// (then column N/2 of both); the two products are packed as
-// col0 + i*colN for one inverse transform.
-template <int N, int HP>
-__device__ __forceinline__ void fwd_both_dc(float2* frame, int dcN, int rowsA, int baseB, int rowsB, int E0,
-                                            int g, float2* scr, const float2* tw, unsigned gmask,
-                                            float scale, float2* a_out, float2* b_out, float2* stash) {
+// OP_FWD_BOTH, DC unit: s is the PSFs' packed column spectrum (columns 0 and
+// N/2 as re/im, transformed like every other column); split it as dc_split
+// does, store both PSF spectrum columns, and form the packed product
+// (column 0's + i * column N/2's) with the image's split spectrum in the DC
+// stash, for one inverse transform.  out may alias the image column.
+template <int N>
+__device__ __forceinline__ void dc_product_split(const float2 (&s)[FftShape<N>::R], const float2* stash,
+                                                 float2* __restrict__ b_out, int g, unsigned gmask, float scale,
+                                                 float2 (&out)[FftShape<N>::R]) {
   constexpr int G = FftShape<N>::G;
   constexpr int R = FftShape<N>::R;
-  float2 v[R];
-#pragma unroll 1
-  for (int half = 0; half < 2; ++half) {
-    const int lcol = half ? dcN : 0;     // local column in the frame
-    const int col = half ? N / 2 : 0;    // bin (spectrum layout)
-    float amax = 0.f, bmax = 0.f;
+  float2 p[R];
+  hermitian_partner<N>(s, p, g, gmask);
 #pragma unroll
-    for (int mm = 0; mm < R; ++mm) {
-      const int r = g + G * mm;
-      v[mm] = make_float2(r < rowsA ? frame[r * HP + lcol].x : 0.f,
-                          r < rowsB ? frame[(baseB + r) * HP + lcol].x : 0.f);
-      amax = fmaxf(amax, fabsf(v[mm].x));
-      bmax = fmaxf(bmax, fabsf(v[mm].y));
+  for (int j = 0; j < R; ++j) {
+    const float2 s0 = make_float2(0.5f * (s[j].x + p[j].x), 0.5f * (s[j].y - p[j].y));
+    const float2 sN = make_float2(0.5f * (s[j].y + p[j].y), 0.5f * (p[j].x - s[j].x));
+    if (b_out) {
+      b_out[g + G * j] = s0;
+      b_out[(long long)(N / 2) * N + g + G * j] = sN;
     }
-    // The two columns can differ in magnitude by orders (image row sums vs
-    // PSF row sums); one complex transform rounds both relative to the
-    // larger, so bring the PSF column to the image's scale by an exact power
-    // of two first and undo it after the split.
-#pragma unroll
-    for (int o = G / 2; o > 0; o >>= 1) {
-      amax = fmaxf(amax, __shfl_xor_sync(gmask, amax, o, G));
-      bmax = fmaxf(bmax, __shfl_xor_sync(gmask, bmax, o, G));
-    }
-    const int e = (amax > 0.f && bmax > 0.f) ? ilogbf(amax) - ilogbf(bmax) : 0;
-    const float up = ldexpf(1.f, e), down = ldexpf(0.5f, -e);  // down folds the split's 1/2
-#pragma unroll
-    for (int mm = 0; mm < R; ++mm) v[mm].y *= up;
-    fft_fwd<N>(v, g, scr, tw, gmask);
-    float2 p[R];
-    hermitian_partner<N>(v, p, g, gmask);
-#pragma unroll
-    for (int j = 0; j < R; ++j) {
-      const float2 sa = make_float2(0.5f * (v[j].x + p[j].x), 0.5f * (v[j].y - p[j].y));
-      const float2 sb = make_float2(down * (v[j].y + p[j].y), down * (p[j].x - v[j].x));
-      if (a_out) a_out[(long long)col * N + g + G * j] = sa;
-      if (b_out) b_out[(long long)col * N + g + G * j] = sb;
-      const float2 pj = cscale(cmul(sa, sb), scale);
-      // column 0's product waits in the stash; column N/2's joins it as i*pj
-      if (half == 0) {
-        stash[j * G + g] = pj;
-      } else {
-        const float2 z0 = stash[j * G + g];
-        v[j] = make_float2(z0.x - pj.y, z0.y + pj.x);
-      }
-    }
+    const float2 p0 = cmul(stash[j * G + g], s0);
+    const float2 pN = cmul(stash[N + j * G + g], sN);
+    out[j] = make_float2((p0.x - pN.y) * scale, (p0.y + pN.x) * scale);
   }
-  fft_inv<N>(v, g, scr, tw, gmask);
-  store_column<N, HP>(frame, 0, true, dcN, 0, E0, g, v);
 }
 
 // One patch `k` of image `b` through the three phases, on this CTA (and its
@@ -662,13 +629,6 @@ __device__ __forceinline__ void eff_patch(const Params& P, int k, long long b, f
   for (int lu = gid; lu < kUnits; lu += NG) {
     const int u = F.rank * kUnits + lu;
     const int col = lu;
-    if constexpr (OP == OP_FWD_BOTH) {
-      if (u == 0) {
-        fwd_both_dc<N, HP>(frame, dcN, rowsA, baseB, P.sf0, P.E0, g, scr, tw, gmask, scale, a_out, b_out,
-                           stash);
-        continue;
-      }
-    }
     // column spectrum of operand A (u == 0: split into the DC stash)
     float2 a[R];
     load_column<N, HP>(frame, col, u == 0, dcN, 0, rowsA, g, a);
@@ -682,17 +642,24 @@ __device__ __forceinline__ void eff_patch(const Params& P, int k, long long b, f
       fft_inv<N>(a, g, scr, tw, gmask);
       store_column<N, HP>(frame, col, u == 0, dcN, 0, P.E0, g, a);
     } else if constexpr (OP == OP_FWD_BOTH) {
-      // u != 0 here: a holds the image column spectrum; transform the PSF
-      // column through the same code and multiply in place
+      // a holds the image column spectrum (u == 0: packed, split into the DC
+      // stash); transform the PSF column through the same code (u == 0: its
+      // columns 0 and N/2 packed the same way) and multiply in place.  The DC
+      // unit diverges from the other lane groups of its warp only in the
+      // splits and the product.
       if (a_out) store_spectrum<N>(a_out, u, g, a, stash);
       float2 s[R];
-      load_column<N, HP>(frame, col, false, dcN, baseB, P.sf0, g, s);
+      load_column<N, HP>(frame, col, u == 0, dcN, baseB, P.sf0, g, s);
       fft_fwd<N>(s, g, scr, tw, gmask);
-      if (b_out) store_spectrum<N>(b_out, u, g, s, stash);
+      if (u != 0) {
+        if (b_out) store_spectrum<N>(b_out, u, g, s, stash);
 #pragma unroll
-      for (int j = 0; j < R; ++j) a[j] = cscale(cmul(a[j], s[j]), scale);
+        for (int j = 0; j < R; ++j) a[j] = cscale(cmul(a[j], s[j]), scale);
+      } else {
+        dc_product_split<N>(s, stash, b_out, g, gmask, scale, a);
+      }
       fft_inv<N>(a, g, scr, tw, gmask);
-      store_column<N, HP>(frame, col, false, dcN, 0, P.E0, g, a);
+      store_column<N, HP>(frame, col, u == 0, dcN, 0, P.E0, g, a);
     } else {
       // adjoints: output 0 = image (conj F-hat, rows sw0), 1 = PSF (conj X-hat, rows sf0);
       // deconv: the same outputs from the regularised division
