@@ -313,10 +313,12 @@ int eff_plan_create(const EffGeom* geom, const float* win0, const float* win1, E
       p.threads = (p.threads / 2 + 31) / 32 * 32;
     }
     // 2-CTA clusters: one lane group per column unit a CTA owns (N/4 units
-    // of G = N/R lanes), at most the compiled maximum, halved while the frame
-    // half plus the exchange scratch does not fit.
+    // of G = N/R lanes) plus a warp in which the DC unit runs alone, at most
+    // the compiled maximum, halved while the frame half plus the exchange
+    // scratch does not fit.
     p.threads2 = g.threads ? g.threads
-                           : std::min(eff::max_threads(p.N), std::max(128, p.N / 4 * (p.N / eff::lane_values(p.N))));
+                           : std::min(eff::max_threads(p.N),
+                                      std::max(128, p.N / 4 * (p.N / eff::lane_values(p.N)) + 32));
     for (;;) {
       size_t worst = 0;
       for (int op = 0; op < eff::kNumOps; ++op) {

@@ -626,7 +626,13 @@ __device__ __forceinline__ void eff_patch(const Params& P, int k, long long b, f
   constexpr int kUnits = N / 2 / CL;  // column units this CTA owns
   constexpr int dcN = Frame<N, CL>::kDcN;
   const float scale = 1.f / (float(N) * float(N));
-  for (int lu = gid; lu < kUnits; lu += NG) {
+  // With a spare warp beyond one lane group per unit, the DC unit (CTA 0's
+  // local unit 0) runs alone in the last warp and units 1.. on groups 0..: its
+  // splits and DC products then serialise no warp of regular units.
+  constexpr int GPW = 32 / G;  // lane groups per warp
+  const bool dc_alone = F.rank == 0 && NG >= kUnits + GPW;
+  const int lu0 = !dc_alone ? gid : (gid == NG - GPW ? 0 : (gid < kUnits - 1 ? gid + 1 : kUnits));
+  for (int lu = lu0; lu < kUnits; lu += dc_alone ? kUnits : NG) {
     const int u = F.rank * kUnits + lu;
     const int col = lu;
     // column spectrum of operand A (u == 0: split into the DC stash)
