@@ -251,7 +251,8 @@ int eff_mu_update(float* x, const float* num, const float* den, float tol, int r
                   int border1, const unsigned* num_max_bits, float floor_rel, unsigned* xmax_bits, int flags,
                   float* zero_f, long long zero_n, void* stream);
 
-/* Uneven batches in one persistent launch (BASELINE's batched workload):
+/* Uneven batches in one persistent launch (e.g. 24 x 256^2 + 24 x 384x512 +
+ * 16 x 1024^2 images):
  * images of up to 8 geometries (one plan each, counts[c] images of plan c,
  * stored back to back per class) are processed by one kernel launch per
  * direction.  The batch keeps a device work list of (class, image, patch)
