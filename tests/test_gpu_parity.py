@@ -100,12 +100,15 @@ CASES = {
     "frame512_cl8": dict(sx=(600, 600), csf=(2, 2), sf=(25, 25), kind="motion"),
     "frame512_same": dict(sx=(400, 440), csf=(2, 2), sf=(25, 21), mode="same"),
     "full_mode_f192": dict(sx=(200, 232), csf=(3, 4), sf=(12, 10), mode="full", sfft=192),
+    # frame 64 (extent 48 x 56): its CTAs have a spare warp for the DC column unit
+    "frame64": dict(sx=(80, 96), csf=(3, 3), sf=(9, 9), kind="motion"),
+    "frame64_same": dict(sx=(70, 90), csf=(3, 4), sf=(9, 7), mode="same"),
 }
 # frame each case runs on
 FRAME = {"cfg1_literal": 128, "cfg1_winaux": 128, "cfg2_literal": 128, "cfg2_winaux": 256,
          "cfg2_winaux_f192": 192, "cfg3_winaux": 256, "cfg3_winaux_f192": 192, "cfg4_mixed": 256,
          "cfg4_mixed_f192": 192, "cfg1_literal_f192": 192, "frame512_cl4": 512, "frame512_cl8a": 512, "frame512_cl8": 512,
-         "frame512_same": 512}
+         "frame512_same": 512, "frame64": 64, "frame64_same": 64}
 
 
 @pytest.fixture(params=[1, 2], ids=["cta", "cluster2"])
