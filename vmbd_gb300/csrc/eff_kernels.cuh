@@ -162,19 +162,15 @@ struct Patch {
   const float* mask;
 };
 
-// Operand value at frame position (r, c).
+// Operand value at frame position (r, c) of the PSF and deconvolution-chop
+// operands (the image and residual operands have row loaders of their own).
 template <int KIND>
 __device__ __forceinline__ float operand(const Params& P, const Patch& T, int r, int c) {
-  if constexpr (KIND == OPND_IMAGE) {
-    if (r >= P.sw0 || c >= P.sw1) return 0.f;
-    const int i = T.m * P.hop0 + r, j = T.n * P.hop1 + c;
-    if (i >= P.sx0 || j >= P.sx1) return 0.f;
-    return window_weight(__ldg(P.win0 + T.m * P.sw0 + r), __ldg(P.win1 + T.n * P.sw1 + c)) *
-           __ldg(T.x + (long long)i * P.sx1 + j);
-  } else if constexpr (KIND == OPND_PSF) {
+  static_assert(KIND == OPND_PSF || KIND == OPND_DCHOP, "image / residual rows: load_image_rows / load_resid_rows");
+  if constexpr (KIND == OPND_PSF) {
     if (r >= P.sf0 || c >= P.sf1) return 0.f;
     return __ldg(T.f + ((long long)T.k * P.sf0 + r) * P.sf1 + c);
-  } else if constexpr (KIND == OPND_DCHOP) {
+  } else {
     // deconv 'xdirect': chop of y placed at frame offset lo (chop_pad_GPU,
     // olaGPU.py:573-580) times the window stack at the frame origin
     // (pad_stack_GPU(ws), :581-584); the supports overlap on [lo, sw)
@@ -183,22 +179,15 @@ __device__ __forceinline__ float operand(const Params& P, const Patch& T, int r,
     if (i >= P.sy0 || j >= P.sy1) return 0.f;
     return window_weight(__ldg(P.win0 + T.m * P.sw0 + r), __ldg(P.win1 + T.n * P.sw1 + c)) *
            __ldg(T.y + (long long)i * P.sy1 + j);
-  } else {
-    if (r < P.lo0 || r >= P.hi0 || c < P.lo1 || c >= P.hi1) return 0.f;
-    const int i = T.m * P.hop0 + r - P.off0, j = T.n * P.hop1 + c - P.off1;
-    if (i < 0 || j < 0 || i >= P.sy0 || j >= P.sy1) return 0.f;
-    const long long o = (long long)i * P.sy1 + j;
-    float v = __ldg(T.y + o);
-    if (T.y_obs) v -= __ldg(T.y_obs + o);
-    if (T.mask) v *= __ldg(T.mask + o);
-    return v;
   }
 }
 
-// Residual rows (ra, ra+1): which rows and which column range [clo, chi)
-// hold data is worked out once per row pair, so the loads are a straight run
-// of independent reads (OBS: minus y_obs; MSK: times the mask).  Same values
-// as operand<OPND_RESID>.
+// Residual rows (ra, ra+1) of the output-side image: frame position (r, c)
+// holds y[i, j] (OBS: minus y_obs[i, j]; MSK: times mask[i, j]) at
+// i = m*hop0 + r - off0, j = n*hop1 + c - off1 inside [lo, hi) of the frame
+// and inside the image, else 0.  Which rows and which column range
+// [clo, chi) hold data is worked out once per row pair, so the loads are a
+// straight run of independent reads.
 template <int N, bool OBS, bool MSK>
 __device__ __forceinline__ void load_resid_rows(const Params& P, const Patch& T, int ra, int g,
                                                 float2 (&v)[FftShape<N>::R]) {
@@ -229,9 +218,10 @@ __device__ __forceinline__ void load_resid_rows(const Params& P, const Patch& T,
   }
 }
 
-// Windowed image rows (ra, ra+1): the rows' window factors and the valid
-// column range are taken once per row pair.  Same values as
-// operand<OPND_IMAGE>.
+// Windowed image rows (ra, ra+1): frame position (r, c) holds
+// window_weight(win0[m][r], win1[n][c]) * x[m*hop0 + r, n*hop1 + c] for
+// r < sw0, c < sw1 inside the image, else 0; the rows' window factors and the
+// valid column range are taken once per row pair.
 template <int N>
 __device__ __forceinline__ void load_image_rows(const Params& P, const Patch& T, int ra, int g,
                                                 float2 (&v)[FftShape<N>::R]) {
