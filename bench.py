@@ -652,8 +652,9 @@ def main():
     w = WORKLOADS[args.workload]
     pixels = w["sx"][0] * w["sx"][1]
     metric = "EFF fwd+adjoint Mpixel/s"
-    config = {"workload": args.workload, "desc": w["desc"], "step": "fused forward (x, f -> y, "
-              "both spectra) + fused adjoint of y - y_obs (loss, both gradients)", "images_per_gpu": 1,
+    config = {"workload": args.workload, "desc": w["desc"], "step": "loss 0.5||EFF(x, f) - y_obs||^2 and both "
+              "gradients: fused residual forward (x, f, y_obs -> r = EFF(x, f) - y_obs, both spectra) + fused "
+              "adjoint of r (loss, both gradients)", "images_per_gpu": 1,
               "l2": "flushed (256 MB write) before every timed step", "parallelism": f"replicas x{world}"}
 
     if args.impl == "reference":
