@@ -185,13 +185,6 @@ def run_ours(args, rank, world, dev):
         # adjoints of the residual with its loss
         plan.loss_grad(x, f, y_obs, loss=loss, gx=gx, gf=gf)
 
-    # the step's two kernels, each on its own (y holds the residual)
-    def k_forward():
-        plan.forward_both(x, f, out=y, xhat_out=xhat, fhat_out=fhat, subtract=y_obs)
-
-    def k_adjoint():
-        plan.adjoint(y, fhat, xhat, loss=loss, gx=gx, gf=gf, residual=True)
-
     flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
     stream = torch.cuda.Stream(device=dev)
     with torch.cuda.stream(stream):
@@ -227,35 +220,12 @@ def run_ours(args, rank, world, dev):
         clk = clocks.stop()
         t_ms = allreduce_max(t_ms, world, dev)
 
-        # per-kernel durations: each kernel (with its memsets) captured in its
-        # own graph, L2 flushed before each replay
-        k_forward()
-        k_adjoint()
-        torch.cuda.synchronize(dev)
-        kern_graphs = {}
-        for name, fn in (("forward", k_forward), ("adjoint", k_adjoint)):
-            gph = torch.cuda.CUDAGraph()
-            with torch.cuda.graph(gph, stream=stream):
-                fn()
-            kern_graphs[name] = gph
-        torch.cuda.synchronize(dev)
-        kern_ms = {}
-        reps = max(5, min(args.steps, 50))
-        for name, gph in kern_graphs.items():
-            tot = 0.0
-            for i in range(reps + 2):
-                flush.fill_(1.0)
-                if name == "adjoint":
-                    k_forward()  # the adjoint reads what the forward leaves in L2
-                a = torch.cuda.Event(enable_timing=True)
-                b = torch.cuda.Event(enable_timing=True)
-                a.record(stream)
-                gph.replay()
-                b.record(stream)
-                torch.cuda.synchronize(dev)
-                if i >= 2:
-                    tot += a.elapsed_time(b)
-            kern_ms[name] = tot / reps
+        # per-kernel durations inside the step: the step's own sequence (memset
+        # of the residual, the fused residual forward clearing the adjoint's
+        # accumulators as a side job, the fused adjoint) captured with timing
+        # events between its kernels, L2 flushed before each replay
+        kern_ms = kernel_times(plan, x, f, y_obs, y, xhat, fhat, gx, gf, loss, flush, stream, dev,
+                               reps=max(5, min(args.steps, 50)))
 
         # unfused per-stage comparator (torch ops + cuFFT), graph-captured
         from vmbd_gb300.unfused import UnfusedEff
@@ -323,6 +293,64 @@ def run_ours(args, rank, world, dev):
                 kern_ms=kern_ms, unfused_ms=unfused_ms, e2e_ms=et, h2d=h2d, d2h=d2h, clocks=clk)
 
 
+def kernel_times(plan, x, f, y_obs, r, xhat, fhat, gx, gf, loss, flush, stream, dev, reps):
+    """Mean device time of the step's forward and adjoint kernels, measured
+    by CUDA events recorded between the kernels of the graph-captured step
+    (event record nodes), each replay after an L2 flush."""
+    import ctypes
+    import torch
+    from vmbd_gb300 import _lib
+    from vmbd_gb300.eff import _ptr
+    L = plan.lib
+    st = ctypes.c_void_p(stream.cuda_stream)
+    nx = int(np.prod(plan.sx))
+
+    def seq(ev):
+        r.zero_()
+        ev[0].record(stream)
+        _lib.check(L.eff_forward_both_ex(plan._h, _ptr(x), _ptr(f), _ptr(y_obs), _ptr(r), _ptr(xhat), _ptr(fhat),
+                                         _lib.OUT_ZEROED, _ptr(gx), nx, _ptr(loss), 1, 1, st))
+        ev[1].record(stream)
+        _lib.check(L.eff_adjoint_ex(plan._h, _ptr(r), None, None, _ptr(fhat), _ptr(xhat), _ptr(gx), _ptr(gf),
+                                    _ptr(loss), _lib.ADJ_EXACT, _lib.OUT_ZEROED | _lib.LOSS_OF_Y, 1, st))
+        ev[2].record(stream)
+
+    tot = {"forward": 0.0, "adjoint": 0.0}
+    try:
+        ev = [torch.cuda.Event(enable_timing=True, external=True) for _ in range(3)]
+        with torch.cuda.stream(stream):
+            seq(ev)
+            torch.cuda.synchronize(dev)
+            gph = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(gph, stream=stream):
+                seq(ev)
+            torch.cuda.synchronize(dev)
+            for i in range(reps + 2):
+                flush.fill_(1.0)
+                gph.replay()
+                torch.cuda.synchronize(dev)
+                if i >= 2:
+                    tot["forward"] += ev[0].elapsed_time(ev[1])
+                    tot["adjoint"] += ev[1].elapsed_time(ev[2])
+        how = "events between the kernels of the graph-captured step"
+    except TypeError:  # a torch without external events: eager, two flushes ahead of the kernels
+        tot = {"forward": 0.0, "adjoint": 0.0}
+        with torch.cuda.stream(stream):
+            for i in range(reps + 2):
+                ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+                flush.fill_(1.0)
+                flush.fill_(2.0)
+                seq(ev)
+                torch.cuda.synchronize(dev)
+                if i >= 2:
+                    tot["forward"] += ev[0].elapsed_time(ev[1])
+                    tot["adjoint"] += ev[1].elapsed_time(ev[2])
+        how = "events around the eagerly launched kernels"
+    out = {k: v / reps for k, v in tot.items()}
+    out["how"] = how
+    return out
+
+
 def profile_run(args, dev):
     """The step, eagerly, warmup + steps times (no graph, no comparators)."""
     import torch
@@ -381,7 +409,7 @@ def profile_run(args, dev):
     print(json.dumps({"profile": args.workload, "steps": args.steps, "warmup": args.warmup}))
 
 
-def run_mfbd(args, dev, n_timed, with_unfused=True):
+def run_mfbd(args, dev, n_timed, with_unfused=True, with_parity=True):
     """Frames/s of the online MFBD loop, one frame per step, graph-captured."""
     import torch
     from vmbd_gb300.mfbd import OnlineMFBD, make_sequence
@@ -448,7 +476,63 @@ def run_mfbd(args, dev, n_timed, with_unfused=True):
 
             ums = timed(unfused, args.warmup + max(5, n_timed // 4))
             out["unfused_gpu"] = {"value": 1e3 / ums, "ms_per_frame": ums, "speedup": ums / ms}
+    if with_parity:
+        out["rel_l2_vs_fp64_oracle"] = mfbd_parity(M, ys[0], x0, f0)
     return out
+
+
+def mfbd_parity(M, y, x0, f0):
+    """Relative L2 of one MFBD frame against the FP64 oracle, from the same
+    start (x0, f0): per step, every kernel output (PSF gradient, F^T(m y),
+    F^T(m F x)) against the oracle applied to the GPU's own state before the
+    step (worst over the frame), and the frame's result (PSFs and image after
+    10 PG + 5 multiplicative steps) against the oracle's own frame."""
+    import torch
+    from oracle import eff64, mfbd64
+    dev = M.device
+    wa = M.winaux
+    g = eff64.Geometry(M.sx, M.sf, wa.csf, wa.sw, wa.nhop, "valid")
+    ws = wa.ws.astype(np.float64)
+    eff64.set_fft_workers(os.cpu_count() or 1)
+
+    def h(t):
+        return t.detach().double().cpu().numpy()
+
+    def rel(a, b):
+        return float(np.linalg.norm(np.asarray(a, np.float64) - b) / np.linalg.norm(b))
+
+    M.x.copy_(x0)
+    M.f.copy_(f0)
+    M.state.fill_(1.0)
+    M.begin_frame(y)
+    torch.cuda.synchronize(dev)
+    yt = h(M.y)
+    mask = (yt < 1).astype(np.float64)
+    x = h(M.x)
+    worst = {"psf_gradient": 0.0, "image_num": 0.0, "image_den": 0.0}
+    for k in range(M.n_pg):
+        fk = h(M.f)
+        M.psf_step(k)
+        torch.cuda.synchronize(dev)
+        g64 = eff64.adjoint_psf(eff64.forward(x, fk, g, ws) - yt, x, g, ws)
+        worst["psf_gradient"] = max(worst["psf_gradient"], rel(h(M.g), g64))
+    f = h(M.f)
+    M.begin_image_steps()
+    torch.cuda.synchronize(dev)
+    worst["image_num"] = rel(h(M.num), eff64.adjoint_image(mask * yt, f, g, ws))
+    for i in range(M.n_mu):
+        xi = h(M.x)
+        M.image_step(i)
+        torch.cuda.synchronize(dev)
+        den64 = eff64.adjoint_image(mask * eff64.forward(xi, f, g, ws), f, g, ws)
+        worst["image_den"] = max(worst["image_den"], rel(h(M.den), den64))
+    xo, fo, _, _ = mfbd64.mfbd_frame(h(x0), h(f0), y.double().cpu().numpy(), g, ws, M.n_pg, M.n_mu,
+                                     state=1.0)
+    eff64.set_fft_workers(None)
+    return {"per_step_worst": worst, "frame_psfs": rel(h(M.f), fo), "frame_image": rel(h(M.x), xo),
+            "note": "per step: each kernel output vs the oracle applied to the GPU's state before the step; "
+                    "frame: PSFs and image after one whole frame vs the oracle's own frame from the same "
+                    "start (rounding propagated through 15 dependent steps)"}
 
 
 def run_deconv(args, dev, n_timed):
@@ -544,7 +628,7 @@ def cfg4_data(dev):
     return plans, counts, xs, fs, yo
 
 
-def run_cfg4(args, dev, n_timed):
+def run_cfg4(args, dev, n_timed, with_parity=True):
     """Images/s of the loss/gradient step over the uneven 64-image batch with
     the autotuner's strategy (every candidate's time is reported)."""
     from vmbd_gb300 import autotune
@@ -554,11 +638,49 @@ def run_cfg4(args, dev, n_timed):
     ms, _, _ = autotune.time_step(runner, xs, fs, yo, reps=max(3, n_timed), warmup=args.warmup)
     n_img = sum(counts)
     items = sum(p.K * c for p, c in zip(plans, counts))
-    return {"value": n_img / (ms * 1e-3), "unit": "images/s", "ms_per_step": ms, "strategy": best,
-            "candidates_ms": {k: v for k, v in times.items() if not k.endswith(":error")},
-            "patches_per_step": items, "frames": [p.N for p in plans],
-            "config": "64 images: 24 x 256^2 (4x4, 15^2 Gaussian), 24 x 384x512 (6x8, 21^2 motion), "
-                      "16 x 1024^2 (12x12, 31^2 motion); loss + both gradients per step"}
+    out = {"value": n_img / (ms * 1e-3), "unit": "images/s", "ms_per_step": ms, "strategy": best,
+           "candidates_ms": {k: v for k, v in times.items() if not k.endswith(":error")},
+           "patches_per_step": items, "frames": [p.N for p in plans],
+           "config": "64 images: 24 x 256^2 (4x4, 15^2 Gaussian), 24 x 384x512 (6x8, 21^2 motion), "
+                     "16 x 1024^2 (12x12, 31^2 motion); loss + both gradients per step"}
+    if with_parity:
+        out["rel_l2_vs_fp64_oracle"] = cfg4_parity(runner.plans, xs, fs, yo)
+    return out
+
+
+def cfg4_parity(plans, xs, fs, yo):
+    """Relative L2 against the FP64 oracle on the first image of each class:
+    the residual forward and both gradients of the step's two kernels (fused
+    residual forward, fused adjoint of that residual) on the plans the chosen
+    strategy runs; the adjoints are compared on the same (GPU) residual."""
+    import torch
+    from oracle import eff64
+    eff64.set_fft_workers(os.cpu_count() or 1)
+
+    def rel(a, b):
+        return float(np.linalg.norm(np.asarray(a, np.float64) - b) / np.linalg.norm(b))
+
+    out = {}
+    for p, x, f, y_obs in zip(plans, xs, fs, yo):
+        xi, fi, yi = x[0].contiguous(), f[0].contiguous(), y_obs[0].contiguous()
+        fh, xh = p.empty_spectrum(), p.empty_spectrum()
+        r = p.forward_both(xi, fi, xhat_out=xh, fhat_out=fh, subtract=yi)
+        loss, gx, gf = p.adjoint(r, fh, xh, residual=True)
+        torch.cuda.synchronize(p.device)
+        wa = p.winaux
+        g = eff64.Geometry(p.sx, p.sf, wa.csf, wa.sw, wa.nhop, "valid")
+        ws = wa.ws.astype(np.float64)
+        xn, fn = xi.double().cpu().numpy(), fi.double().cpu().numpy()
+        yn = yi.double().cpu().numpy()
+        rn = r.double().cpu().numpy()
+        y64 = eff64.forward(xn, fn, g, ws)
+        out[f"{p.sx[0]}x{p.sx[1]}"] = {
+            "forward": rel(rn + yn, y64),
+            "adjoint_image": rel(gx.cpu().numpy(), eff64.adjoint_image(rn, fn, g, ws)),
+            "adjoint_psf": rel(gf.cpu().numpy(), eff64.adjoint_psf(rn, xn, g, ws)),
+            "loss": abs(float(loss) - 0.5 * float(np.sum(rn * rn))) / (0.5 * float(np.sum(rn * rn)))}
+    eff64.set_fft_workers(None)
+    return out
 
 
 def barrier(world):

@@ -6,7 +6,10 @@
  * legacy default stream).  Every entry point returns an EFF_* status and
  * never aborts; eff_last_error() describes the last failure on the calling
  * thread.  Plans are immutable after creation and may be used from several
- * host threads / streams at once.  The compute entry points allocate nothing.
+ * host threads / streams at once.  A plan belongs to the device that was
+ * current at its creation: a call made while another device is current
+ * returns EFF_ERR_INVALID before it queues any work.  The compute entry
+ * points allocate nothing.
  *
  * Geometry (per dim d): image sx, PSF sf, patch grid csf, patch size sw,
  * hop; K = csf0*csf1 patches, patch k = m*csf1 + n at (m*hop0, n*hop1);
@@ -138,19 +141,20 @@ int eff_loss_grad(const EffPlan* plan, const float* x, const float* f, const flo
                   double* loss, float* gx, float* gf, void* workspace, size_t workspace_bytes,
                   int batch, void* stream);
 
-/* eff_loss_grad without a workspace argument, for callers that cannot
- * allocate device memory or pass a workspace: bindings of the reference's
- * cnvinv_objfun / cnvinv_gradfun interface (olaGPU.py:756-811) hand over only
- * the data and the outputs, and some host programs reserve all device memory
- * up front or cannot afford cudaMalloc's implicit synchronisation.  No
- * counterpart in the reference (it allocates fresh GPU arrays on every call).
+/* eff_loss_grad without a workspace argument.  No counterpart in the
+ * reference.  For callers that can neither allocate device memory nor pass a
+ * workspace: an objective/gradient callback whose signature carries only the
+ * data and the outputs, or a host program that reserves all device memory up
+ * front or cannot afford cudaMalloc's implicit synchronisation.
  *
  * The scratch is a static device array of eff_static_scratch_bytes() bytes
  * (16 MiB) that every GPU loading the library keeps until the process exits;
  * larger geometries / batches return EFF_ERR_UNSUPPORTED.  The first call on
- * a device looks up the array's device address (cudaGetSymbolAddress): make
- * it before any stream capture.  All calls share the array; calls whose GPU
- * work overlaps (other streams or threads) race on it.  Allocates nothing. */
+ * a device looks up the array's device address (cudaGetSymbolAddress) and
+ * keeps it: make that first call before any stream capture, and do not call
+ * it again on a device after cudaDeviceReset of that device (the address may
+ * change).  All calls share the array; calls whose GPU work overlaps (other
+ * streams or threads) race on it.  Allocates nothing. */
 size_t eff_static_scratch_bytes(void);
 int eff_loss_grad_static(const EffPlan* plan, const float* x, const float* f, const float* y_obs,
                          double* loss, float* gx, float* gf, int batch, void* stream);
@@ -219,6 +223,14 @@ int eff_forward_ex(const EffPlan* plan, int operand, const float* u, const void*
 int eff_adjoint_ex(const EffPlan* plan, const float* y, const float* y_obs, const float* mask, const void* fhat,
                    const void* xhat, float* gx, float* gf, double* loss, int adj_mode, int flags, int batch,
                    void* stream);
+/* eff_forward_both (sub NULL) / eff_forward_residual (sub = y_obs, not
+ * aliasing y) with the same flags and side jobs as eff_forward_ex.
+ * eff_loss_grad is: memset of its residual buffer, this call with
+ * EFF_OUT_ZEROED clearing gx and loss, eff_adjoint_ex with
+ * EFF_OUT_ZEROED | EFF_LOSS_OF_Y. */
+int eff_forward_both_ex(const EffPlan* plan, const float* x, const float* f, const float* sub, float* y,
+                        void* xhat_out, void* fhat_out, int flags, float* zero_f, long long zero_nf, double* zero_d,
+                        int zero_nd, int batch, void* stream);
 
 /* Online MFBD helpers (vmbd_chimney.py:110-182 with projected-gradient PSF
  * steps, optGPU.py:134-358):
@@ -283,6 +295,11 @@ int eff_batch_adjoint_residual(const EffBatch* batch, const float* const* y, con
  * does not fit in shared memory or when twice the grid still fits on the
  * GPU's SMs at once; 1 always one CTA (where it fits); 2 always a cluster. */
 int eff_set_cluster_mode(int mode);
+
+/* Testing hook: overwrite the device a plan records as its own, so that a
+ * test can check that calls on a mismatched device are refused before any
+ * work is queued.  Not for production use. */
+int eff_test_plan_set_device(EffPlan* plan, int device);
 
 /* Message for the last non-OK status returned on this thread. */
 const char* eff_last_error(void);

@@ -6,6 +6,9 @@ reference's ``gputools.cu`` from where it lies, through a CUDA-execution-model
 shim) with g++ into ``oracle/_ref/libref_gputools.so``.  Does nothing when the
 reference checkout is absent (it exists only where fixtures are generated).
 
+The checkout is the directory named by ``VMBD_REFERENCE_DIR``, else a
+``reference`` directory beside this repository.
+
 Usage: ``python oracle/build_ref.py [reference_dir]``.
 """
 from __future__ import annotations
@@ -17,7 +20,17 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT_DIR = os.path.join(HERE, "_ref")
 LIB = os.path.join(OUT_DIR, "libref_gputools.so")
-DEFAULT_REF = "/root/reference"
+
+def reference_dir() -> str:
+    """Where the reference checkout lies: ``$VMBD_REFERENCE_DIR``, else
+    ``../reference`` relative to the repository root."""
+    env = os.environ.get("VMBD_REFERENCE_DIR")
+    if env:
+        return env
+    return os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
+
+
+DEFAULT_REF = reference_dir()
 
 
 def build(ref_dir: str = DEFAULT_REF, quiet: bool = False) -> str | None:

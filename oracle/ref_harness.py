@@ -42,7 +42,7 @@ from scipy import signal
 
 from . import build_ref
 
-REF_DIR = "/root/reference"
+REF_DIR = build_ref.reference_dir()
 
 # --------------------------------------------------------------------------
 # PyCUDA / pyfft stand-ins

@@ -10,7 +10,8 @@ Entries the reference leaves undefined are stored as NaN: where the patch grid
 covers less than the image, ``crop_gpu2cpu`` reads beyond the overlap-added
 array (no source bounds check in crop_Kernel, gputools.cu:254-263).
 
-Needs the reference checkout; run ``python tests/golden/make_golden.py``.
+Needs the reference checkout; run ``python tests/golden/make_golden.py [case ...]``
+(all cases when none is named).
 """
 from __future__ import annotations
 
@@ -26,6 +27,8 @@ from oracle import ref_harness as rh  # noqa: E402
 from vmbd_gb300 import synth  # noqa: E402
 
 # name: (sx, csf, sf, mode, winaux_sx (None: the image size), psf kind, seed)
+# winaux_sx: the window stack is that of win2winaux on a smaller image whose
+# patch size is the literal one (hop*(csf-1) + sw), used on the full image.
 CASES = {
     "valid_mixed_parity": ((60, 52), (3, 2), (7, 5), "valid", None, "gauss", 11),
     "literal_uncovered": ((64, 64), (2, 2), (9, 9), "valid", (36, 36), "motion", 12),
@@ -33,9 +36,18 @@ CASES = {
     "grid4x4_sf15": ((96, 96), (4, 4), (15, 15), "valid", None, "gauss", 14),
     "wide_nonsquare": ((40, 120), (2, 5), (5, 11), "valid", None, "motion", 15),
 }
+# The two literal workload geometries: 256x256 with a 4x4 grid of 64x64
+# patches and 15x15 Gaussian PSFs, and 512x512 with an 8x8 grid of 96x96
+# patches and 31x31 motion PSFs (both frame 128).  Stored compact: the inputs
+# are regenerated from the seeds by tests/golden/fixtures.py, the fixture keeps
+# their checksums and the reference's outputs.
+LARGE_CASES = {
+    "cfg1_literal": ((256, 256), (4, 4), (15, 15), "valid", (160, 160), "gauss", 31),
+    "cfg2_literal": ((512, 512), (8, 8), (31, 31), "valid", (432, 432), "motion", 32),
+}
 
 
-def make_case(name, sx, csf, sf, mode, wa_sx, kind, seed, gputools, imagetools, olaGPU):
+def make_case(name, sx, csf, sf, mode, wa_sx, kind, seed, gputools, imagetools, olaGPU, compact=False):
     sx = np.array(sx)
     sf = np.array(sf)
     K = int(np.prod(csf))
@@ -48,7 +60,7 @@ def make_case(name, sx, csf, sf, mode, wa_sx, kind, seed, gputools, imagetools, 
     F = olaGPU.OlaGPU(f, sx, mode, wa)
     y = F.cnv(x)
     X = olaGPU.OlaGPU(rh.cua.to_gpu(x), sf, mode, wa)
-    yX = X.cnv(f)
+    yX = None if compact else X.cnv(f)
     r = np.random.default_rng(seed + 200).standard_normal(y.shape).astype(np.float32)
     gx = F.cnvtp(rh.cua.to_gpu(r)).get()
     gf = X.cnvtp(rh.cua.to_gpu(r)).get()
@@ -63,11 +75,19 @@ def make_case(name, sx, csf, sf, mode, wa_sx, kind, seed, gputools, imagetools, 
     ii, jj = np.meshgrid(np.arange(sx[0]), np.arange(sx[1]), indexing="ij")
     undefined_x = (ii >= sxp[0]) | (jj >= sxp[1])
     for a, m in ((y, undefined_y), (yX, undefined_y), (gx, undefined_x)):
-        a[m] = np.nan
+        if a is not None:
+            a[m] = np.nan
     out = dict(sx=sx, sf=sf, csf=np.array(csf), sw=sw, hop=hop, mode=np.array(mode),
-               sfft=np.array(F.sfft_gpu), x=x, f=f, r=r,
-               ws=np.asarray(wa.ws_gpu, np.float32), y=y.astype(np.float32),
-               yX=yX.astype(np.float32), gx=gx.astype(np.float32), gf=gf.astype(np.float32))
+               sfft=np.array(F.sfft_gpu), y=y.astype(np.float32), gx=gx.astype(np.float32),
+               gf=gf.astype(np.float32))
+    if compact:
+        # inputs regenerated from (seed, kind); their checksums pin them
+        out.update(seed=np.array(seed), kind=np.array(kind),
+                   x_sum=np.array([np.sum(x, dtype=np.float64), np.sum(np.square(x, dtype=np.float64))]),
+                   f_sum=np.array([np.sum(f, dtype=np.float64), np.sum(np.square(f, dtype=np.float64))]),
+                   r_sum=np.array([np.sum(r, dtype=np.float64), np.sum(np.square(r, dtype=np.float64))]))
+    else:
+        out.update(x=x, f=f, r=r, ws=np.asarray(wa.ws_gpu, np.float32), yX=yX.astype(np.float32))
     path = os.path.join(HERE, f"ref_{name}.npz")
     np.savez_compressed(path, **out)
     print(f"{name}: sx={tuple(sx)} csf={csf} sf={tuple(sf)} sw={tuple(sw)} hop={tuple(hop)} "
@@ -113,10 +133,16 @@ def make_deconv_case(name, sx, csf, sf, mode, kind, seed, alpha, beta, imagetool
 
 def main():
     gputools, imagetools, olaGPU = rh.load()
+    only = set(sys.argv[1:])
     for name, spec in CASES.items():
-        make_case(name, *spec, gputools, imagetools, olaGPU)
+        if not only or name in only:
+            make_case(name, *spec, gputools, imagetools, olaGPU)
+    for name, spec in LARGE_CASES.items():
+        if not only or name in only:
+            make_case(name, *spec, gputools, imagetools, olaGPU, compact=True)
     for name, spec in DECONV_CASES.items():
-        make_deconv_case(name, *spec, imagetools, olaGPU)
+        if not only or name in only:
+            make_deconv_case(name, *spec, imagetools, olaGPU)
 
 
 if __name__ == "__main__":

@@ -128,3 +128,114 @@ def test_mfbd_frame_graph_replay_matches_eager(cuda):
     torch.cuda.synchronize(cuda)
     assert rel(M2.x.cpu().numpy(), M.x.cpu().numpy()) < 1e-4
     assert rel(M2.f.cpu().numpy(), M.f.cpu().numpy()) < 1e-4
+
+
+# ---------------------------------------------------------------------------
+# The online MFBD workload's geometry (512x512 frames, 8x8 grid of win2winaux
+# 120x120 patches at hop 60, 25x25 drifting motion PSFs, frame 256), three
+# frames, every step checked against the FP64 oracle applied to the GPU's own
+# state before that step.  Each kernel output of a step must match the oracle
+# at relative L2 1e-5; composite quantities (the gradient of a near-converged
+# residual, the BB step size, the updated PSFs and image) get a tolerance
+# derived in the step from the measured input errors and the conditioning of
+# that step, instead of a blanket bound for the iteration.
+# ---------------------------------------------------------------------------
+EPS_FWD = 2e-7   # FP32 forward's relative L2 error bound (measured ~1e-7)
+EPS_PIX = 1e-6   # FP32 transform rounding, absolute, relative to an output's max
+
+
+def _h(t):
+    return t.detach().double().cpu().numpy()
+
+
+def _norm(a):
+    return float(np.linalg.norm(a))
+
+
+def test_mfbd_workload_steps_match_fp64_oracle(cuda):
+    import torch
+    from vmbd_gb300.mfbd import OnlineMFBD, make_sequence
+
+    M = OnlineMFBD((512, 512), (25, 25), (8, 8), n_pg=10, n_mu=5, device=cuda)
+    assert M.plan.N == 256 and M.winaux.sw == (120, 120)
+    _, _, ys = make_sequence(M.plan, 3, seed=11)
+    M.init_latent(ys[:1])
+    g = eff64.Geometry(M.sx, M.sf, M.winaux.csf, M.winaux.sw, M.winaux.nhop, "valid")
+    ws = M.winaux.ws.astype(np.float64)
+    s0, s1 = M.sf
+    worst = {"g": 0.0, "num": 0.0, "den": 0.0}
+    for t in range(ys.shape[0]):
+        M.begin_frame(ys[t])
+        torch.cuda.synchronize(cuda)
+        assert np.abs(_h(M.y) - eff64.edgetaper(ys[t].cpu().numpy(), M.sf)).max() < 1e-6
+        y = _h(M.y)                         # the tapered frame the GPU works on
+        mask = (y < 1).astype(np.float64)
+        x = _h(M.x)
+        for k in range(M.n_pg):
+            f0, fp0, gp0, st0 = _h(M.f), _h(M.f_prev), _h(M.g_prev), float(M.state)
+            M.psf_step(k)
+            torch.cuda.synchronize(cuda)
+            yp = eff64.forward(x, f0, g, ws)
+            r = yp - y
+            g64 = eff64.adjoint_psf(r, x, g, ws)
+            # the residual's relative error is the forward's, scaled by |yp| / |r|
+            e_g = rel(_h(M.g), g64)
+            tol_g = 1e-5 + 4 * EPS_FWD * _norm(yp) / _norm(r)
+            assert e_g <= tol_g, (t, k, e_g, tol_g)
+            worst["g"] = max(worst["g"], e_g)
+            # step size from the same state; its error bound from e_g and the
+            # conditioning of the dot products it divides
+            ng = _norm(g64)
+            if k == 0:
+                xg = eff64.forward(x, g64, g, ws)
+                dots = (float(np.sum(g64 * g64)), 0.0, float(np.sum(xg * xg)))
+                mode, tol_s = 0, 8 * e_g + 8 * EPS_FWD
+            else:
+                dx, dg = f0 - fp0, g64 - gp0
+                dots = (float(np.sum(dx * dx)), float(np.sum(dx * dg)), float(np.sum(dg * dg)))
+                mode = 1 if k % 2 == 1 else 2
+                dd = e_g * ng * _norm(dx) / max(abs(dots[1]), 1e-300)
+                tol_s = 2 * (dd if mode == 1 else dd + 2 * e_g * ng / max(_norm(dg), 1e-300)) + 1e-6
+            s64 = mfbd64.step_size(dots, mode, st0)
+            s_gpu = float(M.state)
+            assert abs(s_gpu - s64) <= tol_s * s64, (t, k, mode, s_gpu, s64, tol_s)
+            # the projected step with the GPU's step size: the projection is
+            # non-expansive, so its error is at most s |dg| plus FP32 rounding
+            f1 = eff64.simplex_project(f0 - s_gpu * g64)
+            tol_f = 2 * s_gpu * e_g * ng / _norm(f1) + 1e-6
+            assert rel(_h(M.f), f1) <= tol_f, (t, k, rel(_h(M.f), f1), tol_f)
+        f = _h(M.f)
+        M.begin_image_steps()
+        torch.cuda.synchronize(cuda)
+        num64 = eff64.adjoint_image(mask * y, f, g, ws)
+        e_num = rel(_h(M.num), num64)
+        assert e_num <= 1e-5, (t, e_num)
+        worst["num"] = max(worst["num"], e_num)
+        num_g = _h(M.num)
+        num_f = np.where(num_g > M.NUM_FLOOR * max(num_g.max(), 0.0), num_g, 0.0)
+        num64f = np.where(num64 > M.NUM_FLOOR * max(num64.max(), 0.0), num64, 0.0)
+        for i in range(M.n_mu):
+            x0 = _h(M.x)
+            M.image_step(i)
+            torch.cuda.synchronize(cuda)
+            den64 = eff64.adjoint_image(mask * eff64.forward(x0, f, g, ws), f, g, ws)
+            den_g = _h(M.den)
+            e_den = rel(den_g, den64)
+            assert e_den <= 1e-5, (t, i, e_den)
+            worst["den"] = max(worst["den"], e_den)
+            # the update kernel's own arithmetic on the GPU's inputs
+            xe = x0 * np.maximum(num_f / (den_g + M.tol), M.tol)
+            xe = np.minimum(xe, xe[s0:xe.shape[0] - s0, s1:xe.shape[1] - s1].max())
+            assert rel(_h(M.x), xe) < 1e-6, (t, i)
+            # against the oracle's update of the same x0: pointwise, an FP32
+            # transform leaves an absolute error of ~EPS_PIX * max on num and
+            # den, so the ratio's relative error is that over num and den
+            x1 = x0 * np.maximum(num64f / (den64 + M.tol), M.tol)
+            x1 = np.minimum(x1, x1[s0:x1.shape[0] - s0, s1:x1.shape[1] - s1].max())
+            sup = num64f > 1e-4 * num64f.max()
+            assert sup.mean() > 0.9
+            bound = x1 * (EPS_PIX * num64f.max() / np.maximum(num64f, 1e-300) +
+                          EPS_PIX * den64.max() / np.maximum(den64, 1e-300))
+            tol_x = 3 * _norm(bound[sup]) / _norm(x1[sup]) + 1e-6
+            assert rel(_h(M.x)[sup], x1[sup]) <= tol_x, (t, i, rel(_h(M.x)[sup], x1[sup]), tol_x)
+    print("mfbd workload per-step worst rel-L2:", worst)

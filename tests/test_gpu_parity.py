@@ -4,8 +4,8 @@ reference's golden vectors and the FP64 oracle.
 Tolerance: relative L2 <= 1e-5 (FP32 kernels vs FP64 oracle), the bound the
 operator's results are stated at.
 """
-import glob
 import os
+import sys
 
 import numpy as np
 import pytest
@@ -15,10 +15,12 @@ from vmbd_gb300 import geometry, synth
 
 pytestmark = pytest.mark.gpu
 TOL = 1e-5
-_ALL = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "ref_*.npz")))
+sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+import fixtures  # noqa: E402
+
 # operator fixtures (cnv / cnvtp) and Fourier-division deconvolution fixtures
-GOLDEN = [p for p in _ALL if not os.path.basename(p).startswith("ref_deconv_")]
-DECONV_GOLDEN = [p for p in _ALL if os.path.basename(p).startswith("ref_deconv_")]
+GOLDEN = fixtures.operator_paths()
+DECONV_GOLDEN = fixtures.deconv_paths()
 
 
 def rel(a, b, mask=None):
@@ -51,9 +53,8 @@ def make(sx, csf, sf, sw=None, hop=None, mode="valid", kind="gauss", seed=0):
 @pytest.mark.parametrize("path", GOLDEN, ids=lambda p: os.path.basename(p))
 def test_olagpu_matches_reference_golden(cuda, path):
     from vmbd_gb300 import OlaGPU
-    z = np.load(path)
-    c = {k: z[k] for k in z.files}
-    mode = str(c["mode"])
+    c = fixtures.load(path)
+    mode = c["mode"]
     wa = geometry.Winaux(tuple(c["sx"]), tuple(c["csf"]), tuple(c["sw"]), tuple(c["hop"]))
     F = OlaGPU(c["f"], tuple(c["sx"]), mode, wa, adjoint="reference")
     X = OlaGPU(c["x"], tuple(c["sf"]), mode, wa, adjoint="reference")
@@ -63,6 +64,7 @@ def test_olagpu_matches_reference_golden(cuda, path):
     assert rel(y, c["y"], m) < TOL
     assert rel(yX, c["y"], m) < TOL
     assert np.all(y[~m] == 0)
+    assert np.all(yX[~m] == 0)
     gx = F.cnvtp(c["r"])
     gf = X.cnvtp(c["r"])
     mx = np.isfinite(c["gx"])

@@ -1,8 +1,8 @@
 """CPU: the FP64 oracle against the reference's golden vectors and against
 its own known-answer properties; the product's host-side geometry against
 the oracle."""
-import glob
 import os
+import sys
 
 import numpy as np
 import pytest
@@ -10,17 +10,16 @@ import pytest
 from oracle import eff64
 from vmbd_gb300 import geometry, synth
 
-_ALL = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "ref_*.npz")))
+sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+import fixtures  # noqa: E402
+
 # operator fixtures (cnv / cnvtp) and Fourier-division deconvolution fixtures
-GOLDEN = [p for p in _ALL if not os.path.basename(p).startswith("ref_deconv_")]
-DECONV_GOLDEN = [p for p in _ALL if os.path.basename(p).startswith("ref_deconv_")]
+GOLDEN = fixtures.operator_paths()
+DECONV_GOLDEN = fixtures.deconv_paths()
 
 
 def load_case(path):
-    z = np.load(path)
-    d = {k: z[k] for k in z.files}
-    d["mode"] = str(d["mode"])
-    d["name"] = os.path.basename(path)[4:-4]
+    d = fixtures.load(path)
     d["geom"] = eff64.Geometry(tuple(d["sx"]), tuple(d["sf"]), tuple(d["csf"]), tuple(d["sw"]),
                                tuple(d["hop"]), d["mode"])
     return d
@@ -36,6 +35,9 @@ def rel(a, b, mask=None):
 
 def test_golden_present():
     assert len(GOLDEN) >= 5
+    names = {os.path.basename(p) for p in GOLDEN}
+    # the literal workload geometries: 256^2 / 4x4 x 64^2 / 15^2 and 512^2 / 8x8 x 96^2 / 31^2
+    assert {"ref_cfg1_literal.npz", "ref_cfg2_literal.npz"} <= names
 
 
 @pytest.mark.parametrize("path", GOLDEN, ids=lambda p: os.path.basename(p))
@@ -47,7 +49,8 @@ def test_oracle_matches_reference_forward(path):
     m = np.isfinite(c["y"])
     # reference computes in FP32: tolerance is FP32 rounding of the pipeline
     assert rel(y, c["y"], m) < 2e-6
-    assert rel(y, c["yX"], m) < 2e-6
+    if "yX" in c:  # X.cnv of the same operator (small cases)
+        assert rel(y, c["yX"], m) < 2e-6
     # the entries the reference leaves undefined are 0 here
     assert np.all(y[~m] == 0)
 

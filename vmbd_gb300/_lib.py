@@ -35,7 +35,8 @@ EXPORTS = (
     "eff_adjoint_masked", "eff_dots3", "eff_pg_step", "eff_mu_update", "eff_max_nonneg",
     "eff_set_cluster_mode", "eff_batch_create", "eff_batch_destroy", "eff_batch_items",
     "eff_batch_forward_both", "eff_batch_adjoint_residual", "eff_deconv_xdirect", "eff_forward_ex",
-    "eff_adjoint_ex", "eff_forward_residual", "eff_batch_forward_residual",
+    "eff_adjoint_ex", "eff_forward_residual", "eff_batch_forward_residual", "eff_test_plan_set_device",
+    "eff_forward_both_ex",
 )
 
 
@@ -94,6 +95,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "eff_pg_step": ([fp, fp, fp, fp, ip, ip, vp, ip, fp, fp, ctypes.c_longlong, vp], ip),
         "eff_max_nonneg": ([fp, ctypes.c_longlong, vp, vp], ip),
         "eff_set_cluster_mode": ([ip], ip),
+        "eff_test_plan_set_device": ([vp, ip], ip),
         "eff_batch_create": ([vp, vp, ip, ctypes.POINTER(vp)], ip),
         "eff_batch_destroy": ([vp], ip),
         "eff_batch_items": ([vp], ip),
@@ -104,6 +106,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
                            ctypes.c_longlong, vp], ip),
         "eff_forward_ex": ([vp, ip, fp, vp, fp, fp, vp, ip, fp, ctypes.c_longlong, vp, ip, ip, vp], ip),
         "eff_adjoint_ex": ([vp, fp, fp, fp, vp, vp, fp, fp, vp, ip, ip, ip, vp], ip),
+        "eff_forward_both_ex": ([vp, fp, fp, fp, fp, vp, vp, ip, fp, ctypes.c_longlong, vp, ip, ip, vp], ip),
         "eff_loss_grad_static": ([vp, fp, fp, fp, vp, fp, fp, ip, vp], ip),
         "eff_deconv_xdirect": ([vp, fp, vp, vp, fp, fp, ctypes.c_float, ctypes.c_float, ip, vp], ip),
     }

@@ -142,6 +142,10 @@ def tune(plans, counts, xs, fs, ys_obs, cands=None):
         except Exception as e:
             times[c] = float("inf")
             times[c + ":error"] = str(e)[:200]
-    best = min((c for c in cands if times[c] != float("inf")), key=lambda c: times[c])
+    ran = [c for c in cands if times[c] != float("inf")]
+    if not ran:
+        errors = {k: v for k, v in times.items() if k.endswith(":error")}
+        raise RuntimeError(f"no batch strategy could run on this batch: {errors}")
+    best = min(ran, key=lambda c: times[c])
     _CACHE[key] = (best, times)
     return best, times

@@ -97,6 +97,7 @@ struct EffBatch {
   eff::Item* items;
   int n_items;
   int grid;
+  int device;  // of every plan and of the work list
 };
 
 namespace {
@@ -119,6 +120,7 @@ int eff_batch_create(const EffPlan* const* plans, const int* counts, int n_class
   std::vector<std::pair<int, int>> order;  // (frame, class)
   for (int c = 0; c < n_classes; ++c) {
     if (!plans[c] || counts[c] < 1) return fail(EFF_ERR_INVALID, "bad plan or count");
+    if (int s = eff::check_plan_device(plans[c])) return s;
     B.plans[c] = plans[c];
     B.counts[c] = counts[c];
     int n = 0;
@@ -138,6 +140,7 @@ int eff_batch_create(const EffPlan* const* plans, const int* counts, int n_class
   cudaError_t e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (e != cudaSuccess) return fail(EFF_ERR_CUDA, std::string("device query: ") + cudaGetErrorString(e));
+  B.device = dev;
   B.grid = std::max(2, (sms / 2) * 2);
   B.n_items = (int)items.size();
   e = cudaMalloc(&B.items, sizeof(eff::Item) * items.size());
@@ -175,6 +178,9 @@ int batch_run(const EffBatch* B, int op, const float* const* x, const float* con
               const float* const* y_obs, const void* const* spec0, const void* const* spec1, float* const* out0,
               float* const* out1, void* const* a_out, void* const* b_out, double* const* loss, void* stream) {
   if (!B) return set_error(EFF_ERR_INVALID, "null batch");
+  // the plans' tables and the work list live on the batch's device
+  for (int c = 0; c < B->n; ++c)
+    if (int s = check_plan_device(B->plans[c])) return s;
   ClassTable T;
   std::memset(&T, 0, sizeof(T));
   T.n = B->n;

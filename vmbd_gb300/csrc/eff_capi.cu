@@ -131,10 +131,23 @@ int run(const EffPlan* p, int op, const eff::Params& P, int batch, void* stream)
   return EFF_OK;
 }
 
+// The plan's tables live on the device that was current at eff_plan_create;
+// a kernel launched while another device is current would read them through
+// addresses of that other device.  Refused before any memset or launch.
+int check_device(const EffPlan* p) {
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  if (dev != p->device)
+    return fail(EFF_ERR_INVALID, "plan was created on device " + std::to_string(p->device) + " but device " +
+                                     std::to_string(dev) + " is current");
+  return EFF_OK;
+}
+
 int check_plan(const EffPlan* p, int batch) {
   if (!p) return fail(EFF_ERR_INVALID, "null plan");
   if (batch < 1 || batch > 65535) return fail(EFF_ERR_INVALID, "batch must be in [1, 65535]");
-  return EFF_OK;
+  return check_device(p);
 }
 
 // zeroed: gx and loss were already zeroed on the stream (by the fused forward).
@@ -247,6 +260,13 @@ int eff::plan_params(const EffPlan* plan, eff::Params* P, int* N) {
 }
 
 int eff::plan_patches(const EffPlan* plan) { return plan ? plan->K : 0; }
+
+int eff::plan_device(const EffPlan* plan) { return plan ? plan->device : -1; }
+
+int eff::check_plan_device(const EffPlan* plan) {
+  if (!plan) return fail(EFF_ERR_INVALID, "null plan");
+  return check_device(plan);
+}
 
 extern "C" {
 
@@ -601,6 +621,37 @@ int eff_forward_residual(const EffPlan* plan, const float* x, const float* f, co
   return run(plan, eff::OP_FWD_BOTH, P, batch, stream);
 }
 
+int eff_forward_both_ex(const EffPlan* plan, const float* x, const float* f, const float* sub, float* y,
+                        void* xhat_out, void* fhat_out, int flags, float* zero_f, long long zero_nf, double* zero_d,
+                        int zero_nd, int batch, void* stream) {
+  if (int s = check_plan(plan, batch)) return s;
+  if (!x || !f || !y) return fail(EFF_ERR_INVALID, "null argument");
+  if (sub == y) return fail(EFF_ERR_INVALID, "sub must not alias y");
+  if ((flags & ~EFF_OUT_ZEROED) || zero_nf < 0 || zero_nd < 0 || (zero_nf > 0 && !zero_f) || (zero_nd > 0 && !zero_d))
+    return fail(EFF_ERR_INVALID, "bad argument");
+  eff::Params P = base_params(plan);
+  P.x = x;
+  P.f = f;
+  P.out0 = y;
+  P.out0_bs = P.y_bs;
+  P.a_out = static_cast<float2*>(xhat_out);
+  P.b_out = static_cast<float2*>(fhat_out);
+  if (sub) {
+    P.pf = reinterpret_cast<const char*>(sub);
+    P.pf_bytes = (long long)sizeof(float) * P.y_bs;
+    P.sub = sub;
+  }
+  P.zero_f = zero_nf > 0 ? zero_f : nullptr;
+  P.zero_nf = zero_nf;
+  P.zero_d = zero_nd > 0 ? zero_d : nullptr;
+  P.zero_nd = zero_nd;
+  if (!(flags & EFF_OUT_ZEROED)) {
+    cudaError_t e = cudaMemsetAsync(y, 0, sizeof(float) * P.y_bs * batch, static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+  }
+  return run(plan, eff::OP_FWD_BOTH, P, batch, stream);
+}
+
 size_t eff_loss_grad_workspace_bytes(const EffPlan* plan, int batch) {
   if (!plan || batch < 1) return 0;
   return workspace_layout(plan, batch).total;
@@ -681,6 +732,12 @@ int eff_mu_update(float* x, const float* num, const float* den, float tol, int r
                                         floor_rel, xmax_bits, (flags & EFF_OUT_ZEROED) != 0, zero_f, zero_n,
                                         static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(e, "mu_update launch");
+  return EFF_OK;
+}
+
+int eff_test_plan_set_device(EffPlan* plan, int device) {
+  if (!plan) return fail(EFF_ERR_INVALID, "null plan");
+  plan->device = device;
   return EFF_OK;
 }
 

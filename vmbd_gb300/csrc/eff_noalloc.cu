@@ -14,7 +14,9 @@
 // the process exits.  Host code cannot use the array's name as a device
 // address, so the first call on each device looks the address up with
 // cudaGetSymbolAddress (with that device current) and caches it; make that
-// first call before any stream capture begins.  All calls share the array and
+// first call before any stream capture begins, and do not use the entry point
+// on a device after cudaDeviceReset of that device (the module is loaded
+// again and the cached address may be stale).  All calls share the array and
 // it keeps the last call's contents: the step clears what must start at zero
 // (the forward output and the loss) itself, and two calls whose GPU work
 // overlaps (different streams, different host threads) race on it.
@@ -64,6 +66,9 @@ int eff_loss_grad_static(const EffPlan* plan, const float* x, const float* f, co
                          double* loss, float* gx, float* gf, int batch, void* stream) {
   if (!plan) return eff::set_error(EFF_ERR_INVALID, "null plan");
   if (batch < 1) return eff::set_error(EFF_ERR_INVALID, "batch must be >= 1");
+  // the scratch address is looked up on the current device, the plan's
+  // tables live on the plan's device: they must be the same device
+  if (int s = eff::check_plan_device(plan)) return s;
   const size_t need = eff_loss_grad_workspace_bytes(plan, batch);
   if (need > kStaticScratchBytes)
     return eff::set_error(EFF_ERR_UNSUPPORTED,

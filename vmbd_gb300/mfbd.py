@@ -93,62 +93,87 @@ class OnlineMFBD:
     def frame(self, y: torch.Tensor = None) -> None:
         """Process one frame (``y`` is copied into the static input buffer;
         pass None when it is already there, e.g. under graph replay)."""
-        L, st, P = self.lib, _stream(self.device), self.plan
+        self.begin_frame(y)
+        for k in range(self.n_pg):
+            self.psf_step(k)
+        self.begin_image_steps()
+        for i in range(self.n_mu):
+            self.image_step(i)
+
+    # The frame's stages, in the order frame() runs them (each only enqueues
+    # work on the current stream).  Accumulated outputs are cleared as side
+    # jobs of earlier kernels that do not touch them (EFF_OUT_ZEROED on their
+    # own call), so the frame graph has three memset nodes instead of ~40.
+    def begin_frame(self, y: torch.Tensor = None) -> None:
+        """Edgetaper of y, the saturation mask, the X object of x."""
         if y is not None:
             self.y.copy_(y)
         if self.taper is not None:
             self.taper(self.y)
         torch.lt(self.y, 1.0, out=self.mask)  # bool -> float via out dtype
+        self.plan.image_spectrum(self.x, out=self.xhat)
+
+    def psf_step(self, k: int) -> None:
+        """PSF step k: g = X^T (X f - y), step size (k = 0: exact line
+        search; then BB1 / BB2 alternately), f <- P_simplex(f - s g); the
+        previous f and g move to f_prev / g_prev, s to ``state``."""
+        L, st, P = self.lib, _stream(self.device), self.plan
         K, n = self.winaux.K, self.n
         ny = self.sy[0] * self.sy[1]
-        # Accumulated outputs are cleared as side jobs of earlier kernels that
-        # do not touch them (EFF_OUT_ZEROED on their own call), so the frame
-        # graph has three memset nodes instead of ~40.
-        OZ, nx = _lib.OUT_ZEROED, self.sx[0] * self.sx[1]
+        OZ = _lib.OUT_ZEROED
         amode = _lib.ADJ_EXACT if self.adjoint == "exact" else _lib.ADJ_REFERENCE
-        # --- PSF estimation: X object of the current latent image --------
-        P.image_spectrum(self.x, out=self.xhat)
-        for k in range(self.n_pg):
-            # residual X f - y into y_pred (cleared by the previous PSF step;
-            # memset at k = 0); side jobs: clear dots (and yg at k = 0)
-            self._check(L.eff_forward_ex(P._h, _lib.OPERAND_PSF, _ptr(self.f), _ptr(self.xhat), _ptr(self.ypred),
-                                         _ptr(self.y), None, OZ if k > 0 else 0, _ptr(self.yg) if k == 0 else None,
-                                         ny if k == 0 else 0, _ptr(self.dots), 3, 1, st))
-            # g = X^T (X f - y); the BB / exact-line-search steps need no objective value
-            self._check(L.eff_adjoint_ex(P._h, _ptr(self.ypred), None, None, None, _ptr(self.xhat),
-                                         None, _ptr(self.g), None, amode, 0, 1, st))
-            if k == 0:
-                self._check(L.eff_forward_ex(P._h, _lib.OPERAND_PSF, _ptr(self.g), _ptr(self.xhat),
-                                             _ptr(self.yg), None, None, OZ, None, 0, None, 0, 1, st))
-                self._check(L.eff_dots3(_ptr(self.g), None, K * n, _ptr(self.yg), None, ny,
-                                        _ptr(self.dots), OZ, st))
-                mode = 0
-            else:
-                self._check(L.eff_dots3(_ptr(self.f), _ptr(self.f_prev), K * n, _ptr(self.g),
-                                        _ptr(self.g_prev), K * n, _ptr(self.dots), OZ, st))
-                mode = 1 if k % 2 == 1 else 2
-            # side job: clear y_pred for the next forward
-            self._check(L.eff_pg_step(_ptr(self.f), _ptr(self.g), _ptr(self.f_prev), _ptr(self.g_prev),
-                                      K, n, _ptr(self.dots), mode, _ptr(self.state), _ptr(self.ypred), ny, st))
-        # --- latent image: F object of the new PSFs ------------------------
+        # residual X f - y into y_pred (cleared by the previous PSF step;
+        # memset at k = 0); side jobs: clear dots (and yg at k = 0)
+        self._check(L.eff_forward_ex(P._h, _lib.OPERAND_PSF, _ptr(self.f), _ptr(self.xhat), _ptr(self.ypred),
+                                     _ptr(self.y), None, OZ if k > 0 else 0, _ptr(self.yg) if k == 0 else None,
+                                     ny if k == 0 else 0, _ptr(self.dots), 3, 1, st))
+        # g = X^T (X f - y); the BB / exact-line-search steps need no objective value
+        self._check(L.eff_adjoint_ex(P._h, _ptr(self.ypred), None, None, None, _ptr(self.xhat),
+                                     None, _ptr(self.g), None, amode, 0, 1, st))
+        if k == 0:
+            self._check(L.eff_forward_ex(P._h, _lib.OPERAND_PSF, _ptr(self.g), _ptr(self.xhat),
+                                         _ptr(self.yg), None, None, OZ, None, 0, None, 0, 1, st))
+            self._check(L.eff_dots3(_ptr(self.g), None, K * n, _ptr(self.yg), None, ny,
+                                    _ptr(self.dots), OZ, st))
+            mode = 0
+        else:
+            self._check(L.eff_dots3(_ptr(self.f), _ptr(self.f_prev), K * n, _ptr(self.g),
+                                    _ptr(self.g_prev), K * n, _ptr(self.dots), OZ, st))
+            mode = 1 if k % 2 == 1 else 2
+        # side job: clear y_pred for the next forward
+        self._check(L.eff_pg_step(_ptr(self.f), _ptr(self.g), _ptr(self.f_prev), _ptr(self.g_prev),
+                                  K, n, _ptr(self.dots), mode, _ptr(self.state), _ptr(self.ypred), ny, st))
+
+    def begin_image_steps(self) -> None:
+        """F object of the new PSFs, num = F^T(m y) and its maximum."""
+        L, st, P = self.lib, _stream(self.device), self.plan
+        nx = self.sx[0] * self.sx[1]
+        amode = _lib.ADJ_EXACT if self.adjoint == "exact" else _lib.ADJ_REFERENCE
         P.psf_spectrum(self.f, out=self.fhat)
         self._check(L.eff_adjoint_masked(P._h, _ptr(self.y), _ptr(self.mask), _ptr(self.fhat), None,
                                          _ptr(self.num), None, amode, 1, st))
         self._check(L.eff_max_nonneg(_ptr(self.num), nx, _ptr(self.nummax), st))
-        for i in range(self.n_mu):
-            # y_pred = F x (y_pred cleared by the previous PSF step or image
-            # step); side job: clear den and the interior-maximum word
-            self._check(L.eff_forward_ex(P._h, _lib.OPERAND_IMAGE, _ptr(self.x), _ptr(self.fhat),
-                                         _ptr(self.ypred), None, None, OZ if (i > 0 or self.n_pg > 0) else 0,
-                                         _ptr(self._denx), nx + 1, None, 0, 1, st))
-            self._check(L.eff_adjoint_ex(P._h, _ptr(self.ypred), None, _ptr(self.mask), _ptr(self.fhat), None,
-                                         _ptr(self.den), None, None, amode, OZ, 1, st))
-            last = i == self.n_mu - 1
-            self._check(L.eff_mu_update(_ptr(self.x), _ptr(self.num), _ptr(self.den),
-                                        ctypes.c_float(self.tol), self.sx[0], self.sx[1], self.sf[0],
-                                        self.sf[1], _ptr(self.nummax), ctypes.c_float(self.NUM_FLOOR),
-                                        _ptr(self.xmax), OZ, None if last else _ptr(self.ypred),
-                                        0 if last else ny, st))
+
+    def image_step(self, i: int) -> None:
+        """Image step i: den = F^T(m F x), x *= max(num / (den + tol), tol),
+        x <= max of x over the interior."""
+        L, st, P = self.lib, _stream(self.device), self.plan
+        ny = self.sy[0] * self.sy[1]
+        OZ, nx = _lib.OUT_ZEROED, self.sx[0] * self.sx[1]
+        amode = _lib.ADJ_EXACT if self.adjoint == "exact" else _lib.ADJ_REFERENCE
+        # y_pred = F x (y_pred cleared by the previous PSF step or image
+        # step); side job: clear den and the interior-maximum word
+        self._check(L.eff_forward_ex(P._h, _lib.OPERAND_IMAGE, _ptr(self.x), _ptr(self.fhat),
+                                     _ptr(self.ypred), None, None, OZ if (i > 0 or self.n_pg > 0) else 0,
+                                     _ptr(self._denx), nx + 1, None, 0, 1, st))
+        self._check(L.eff_adjoint_ex(P._h, _ptr(self.ypred), None, _ptr(self.mask), _ptr(self.fhat), None,
+                                     _ptr(self.den), None, None, amode, OZ, 1, st))
+        last = i == self.n_mu - 1
+        self._check(L.eff_mu_update(_ptr(self.x), _ptr(self.num), _ptr(self.den),
+                                    ctypes.c_float(self.tol), self.sx[0], self.sx[1], self.sf[0],
+                                    self.sf[1], _ptr(self.nummax), ctypes.c_float(self.NUM_FLOOR),
+                                    _ptr(self.xmax), OZ, None if last else _ptr(self.ypred),
+                                    0 if last else ny, st))
 
     def launches_per_frame(self) -> int:
         """Kernels of this library one frame launches."""
