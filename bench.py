@@ -227,6 +227,33 @@ def run_ours(args, rank, world, dev):
         kern_ms = kernel_times(plan, x, f, y_obs, y, xhat, fhat, gx, gf, loss, flush, stream, dev,
                                reps=max(5, min(args.steps, 50)))
 
+        # the same step on a deterministic plan (fixed-order gather overlap-add)
+        det_ms = None
+        try:
+            dplan = EffPlan(wa, w["sf"], "valid", device=dev, deterministic=True)
+            dstep = lambda: dplan.loss_grad(x, f, y_obs, loss=loss, gx=gx, gf=gf)  # noqa: E731
+            for _ in range(3):
+                dstep()
+            torch.cuda.synchronize(dev)
+            dg = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(dg, stream=stream):
+                dstep()
+            torch.cuda.synchronize(dev)
+            dt = 0.0
+            for i in range(args.warmup + args.steps):
+                flush.fill_(1.0)
+                a = torch.cuda.Event(enable_timing=True)
+                b = torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                dg.replay()
+                b.record(stream)
+                torch.cuda.synchronize(dev)
+                if i >= args.warmup:
+                    dt += a.elapsed_time(b)
+            det_ms = dt / args.steps
+        except Exception as e:  # reported, not fatal to the headline line
+            det_ms = repr(e)[:200]
+
         # unfused per-stage comparator (torch ops + cuFFT), graph-captured
         from vmbd_gb300.unfused import UnfusedEff
         U = UnfusedEff(wa, w["sf"], N=N, device=dev)
@@ -290,13 +317,17 @@ def run_ours(args, rank, world, dev):
     torch.cuda.synchronize(dev)
     return dict(plan=plan, wa=wa, w=w, x_np=x_np, f_np=f_np, y_obs=y_obs.cpu().numpy(),
                 gx=gx.cpu().numpy(), gf=gf.cpu().numpy(), y=y.cpu().numpy(), t_ms=t_ms,
-                kern_ms=kern_ms, unfused_ms=unfused_ms, e2e_ms=et, h2d=h2d, d2h=d2h, clocks=clk)
+                kern_ms=kern_ms, unfused_ms=unfused_ms, e2e_ms=et, h2d=h2d, d2h=d2h, clocks=clk, det_ms=det_ms)
 
 
 def kernel_times(plan, x, f, y_obs, r, xhat, fhat, gx, gf, loss, flush, stream, dev, reps):
-    """Mean device time of the step's forward and adjoint kernels, measured
-    by CUDA events recorded between the kernels of the graph-captured step
-    (event record nodes), each replay after an L2 flush."""
+    """Device time each kernel adds to the graph-captured step: the step's own
+    sequence (memset of the residual, the fused residual forward clearing the
+    adjoint's accumulators as a side job, the fused adjoint) captured as three
+    graphs -- the memset, memset + forward, the whole step -- each replayed
+    after an L2 flush and timed with CUDA events; forward = T(memset + forward)
+    - T(memset), adjoint = T(step) - T(memset + forward).  Each includes its
+    launch gap inside the graph."""
     import ctypes
     import torch
     from vmbd_gb300 import _lib
@@ -305,50 +336,40 @@ def kernel_times(plan, x, f, y_obs, r, xhat, fhat, gx, gf, loss, flush, stream, 
     st = ctypes.c_void_p(stream.cuda_stream)
     nx = int(np.prod(plan.sx))
 
-    def seq(ev):
+    def seq(n):
         r.zero_()
-        ev[0].record(stream)
-        _lib.check(L.eff_forward_both_ex(plan._h, _ptr(x), _ptr(f), _ptr(y_obs), _ptr(r), _ptr(xhat), _ptr(fhat),
-                                         _lib.OUT_ZEROED, _ptr(gx), nx, _ptr(loss), 1, 1, st))
-        ev[1].record(stream)
-        _lib.check(L.eff_adjoint_ex(plan._h, _ptr(r), None, None, _ptr(fhat), _ptr(xhat), _ptr(gx), _ptr(gf),
-                                    _ptr(loss), _lib.ADJ_EXACT, _lib.OUT_ZEROED | _lib.LOSS_OF_Y, 1, st))
-        ev[2].record(stream)
+        if n >= 1:
+            _lib.check(L.eff_forward_both_ex(plan._h, _ptr(x), _ptr(f), _ptr(y_obs), _ptr(r), _ptr(xhat),
+                                             _ptr(fhat), _lib.OUT_ZEROED, _ptr(gx), nx, _ptr(loss), 1, 1, st))
+        if n >= 2:
+            _lib.check(L.eff_adjoint_ex(plan._h, _ptr(r), None, None, _ptr(fhat), _ptr(xhat), _ptr(gx), _ptr(gf),
+                                        _ptr(loss), _lib.ADJ_EXACT, _lib.OUT_ZEROED | _lib.LOSS_OF_Y, 1, st))
 
-    tot = {"forward": 0.0, "adjoint": 0.0}
-    try:
-        ev = [torch.cuda.Event(enable_timing=True, external=True) for _ in range(3)]
-        with torch.cuda.stream(stream):
-            seq(ev)
+    graphs = []
+    with torch.cuda.stream(stream):
+        for n in range(3):
+            seq(n)
             torch.cuda.synchronize(dev)
             gph = torch.cuda.CUDAGraph()
             with torch.cuda.graph(gph, stream=stream):
-                seq(ev)
-            torch.cuda.synchronize(dev)
-            for i in range(reps + 2):
+                seq(n)
+            graphs.append(gph)
+        torch.cuda.synchronize(dev)
+        tot = [0.0, 0.0, 0.0]
+        for i in range(reps + 2):
+            for n, gph in enumerate(graphs):  # interleaved, so that all three see the same conditions
                 flush.fill_(1.0)
+                a = torch.cuda.Event(enable_timing=True)
+                b = torch.cuda.Event(enable_timing=True)
+                a.record(stream)
                 gph.replay()
+                b.record(stream)
                 torch.cuda.synchronize(dev)
                 if i >= 2:
-                    tot["forward"] += ev[0].elapsed_time(ev[1])
-                    tot["adjoint"] += ev[1].elapsed_time(ev[2])
-        how = "events between the kernels of the graph-captured step"
-    except TypeError:  # a torch without external events: eager, two flushes ahead of the kernels
-        tot = {"forward": 0.0, "adjoint": 0.0}
-        with torch.cuda.stream(stream):
-            for i in range(reps + 2):
-                ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
-                flush.fill_(1.0)
-                flush.fill_(2.0)
-                seq(ev)
-                torch.cuda.synchronize(dev)
-                if i >= 2:
-                    tot["forward"] += ev[0].elapsed_time(ev[1])
-                    tot["adjoint"] += ev[1].elapsed_time(ev[2])
-        how = "events around the eagerly launched kernels"
-    out = {k: v / reps for k, v in tot.items()}
-    out["how"] = how
-    return out
+                    tot[n] += a.elapsed_time(b)
+    t = [v / reps for v in tot]
+    return {"forward": t[1] - t[0], "adjoint": t[2] - t[1], "memset": t[0],
+            "how": "differences of graph-replayed prefixes of the step (memset | + forward | + adjoint)"}
 
 
 def profile_run(args, dev):
@@ -851,6 +872,10 @@ def main():
                         "speedup": R["unfused_ms"] / ms},
         "e2e": {"value": world * pixels / (e2e_ms * 1e-3) / 1e6, "unit": "Mpixel/s",
                 "ms_per_step": e2e_ms, "h2d_bytes_per_step": R["h2d"], "d2h_bytes_per_step": R["d2h"]},
+        "deterministic": ({"ms_per_step": R["det_ms"], "vs_atomic": R["det_ms"] / ms,
+                           "what": "same step on a plan with the fixed-order gather overlap-add (bit-identical "
+                                   "repeats): forward + gather + adjoint + gather"}
+                          if isinstance(R["det_ms"], float) else {"error": R["det_ms"]}),
         "gpu_launches": 2 * args.steps,
         "clocks": clk,
     }

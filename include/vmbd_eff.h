@@ -68,7 +68,19 @@ typedef struct EffGeom {
   int threads; /* CTA size, a multiple of 32 up to the frame's maximum (512; 384 for frame
                   192, 576 for 256, 256 for 512); 0 = the largest that fits.  Lowered to
                   fit shared memory. */
+  int flags;   /* EFF_GEOM_* */
 } EffGeom;
+
+/* EffGeom.flags: deterministic overlap-add.  The kernels store each patch's
+ * output tile and a gather kernel sums the tiles covering each pixel in a
+ * fixed order (patch rows, then patch columns), as the reference's
+ * ola_Kernel_test does (gputools.cu:276-314); the loss is summed in a fixed
+ * order too.  Repeated calls give bit-identical outputs.  The plan then owns
+ * a device scratch of one image's tiles (K * max(E0 E1, sw0 sw1) floats):
+ * calls on several streams at once race on it, and batched calls run image
+ * by image.  Costs one extra kernel per overlap-added output.  Not accepted
+ * by eff_batch_create. */
+#define EFF_GEOM_DETERMINISTIC 1
 
 typedef struct EffPlan EffPlan;
 
@@ -295,6 +307,20 @@ int eff_batch_adjoint_residual(const EffBatch* batch, const float* const* y, con
  * does not fit in shared memory or when twice the grid still fits on the
  * GPU's SMs at once; 1 always one CTA (where it fits); 2 always a cluster. */
 int eff_set_cluster_mode(int mode);
+
+/* Error bits the plan's kernels recorded on the device (EFF_DEVERR_*), read
+ * after waiting for all work on the current device; clear != 0 resets them.
+ * EFF_DEVERR_COPY_TIMEOUT: a bulk copy into shared memory did not complete
+ * within the kernel's wait limit (that call's results are not valid). */
+#define EFF_DEVERR_COPY_TIMEOUT 1
+int eff_plan_device_errors(const EffPlan* plan, int* flags, int clear);
+
+/* 1: kernels that multiply by cached spectra (adjoints, forwards from a
+ * cached spectrum, deconvolution) copy their columns of the spectra into
+ * shared memory with the bulk-copy engine at kernel start, where the CTA's
+ * shared memory allows; 0 (default): they read them from global memory,
+ * where a step's spectra sit in L2.  For all plans of the process. */
+int eff_set_spectrum_staging(int on);
 
 /* Testing hook: overwrite the device a plan records as its own, so that a
  * test can check that calls on a mismatched device are refused before any

@@ -38,9 +38,11 @@ CASES = {
 }
 # The two literal workload geometries: 256x256 with a 4x4 grid of 64x64
 # patches and 15x15 Gaussian PSFs, and 512x512 with an 8x8 grid of 96x96
-# patches and 31x31 motion PSFs (both frame 128).  Stored compact: the inputs
-# are regenerated from the seeds by tests/golden/fixtures.py, the fixture keeps
-# their checksums and the reference's outputs.
+# patches and 31x31 motion PSFs (both frame 128).  Stored compact: the image
+# and PSFs are stored (the generators' rounding differs between machines),
+# the residual is regenerated from its seed (numpy's generator is the same
+# everywhere) and pinned by a checksum, the window stack is the host
+# geometry's.
 LARGE_CASES = {
     "cfg1_literal": ((256, 256), (4, 4), (15, 15), "valid", (160, 160), "gauss", 31),
     "cfg2_literal": ((512, 512), (8, 8), (31, 31), "valid", (432, 432), "motion", 32),
@@ -81,10 +83,8 @@ def make_case(name, sx, csf, sf, mode, wa_sx, kind, seed, gputools, imagetools, 
                sfft=np.array(F.sfft_gpu), y=y.astype(np.float32), gx=gx.astype(np.float32),
                gf=gf.astype(np.float32))
     if compact:
-        # inputs regenerated from (seed, kind); their checksums pin them
-        out.update(seed=np.array(seed), kind=np.array(kind),
-                   x_sum=np.array([np.sum(x, dtype=np.float64), np.sum(np.square(x, dtype=np.float64))]),
-                   f_sum=np.array([np.sum(f, dtype=np.float64), np.sum(np.square(f, dtype=np.float64))]),
+        # the residual is regenerated from the seed; its checksum pins it
+        out.update(x=x, f=f, seed=np.array(seed),
                    r_sum=np.array([np.sum(r, dtype=np.float64), np.sum(np.square(r, dtype=np.float64))]))
     else:
         out.update(x=x, f=f, r=r, ws=np.asarray(wa.ws_gpu, np.float32), yX=yX.astype(np.float32))

@@ -88,3 +88,12 @@ def test_adjoint_ex_flags_validate_without_gpu():
                             8, 1, None) == _lib.EFF_ERR_INVALID
     assert L.eff_forward_residual(None, dummy, dummy, dummy, dummy, None, None, 1, None) == _lib.EFF_ERR_INVALID
     assert L.eff_forward_residual(None, None, None, None, None, None, None, 1, None) == _lib.EFF_ERR_INVALID
+
+
+def test_debug_library_exports_every_symbol():
+    # the bounds-checked variant has the same C ABI
+    path = build.build(debug=True)
+    lib = ctypes.CDLL(path)
+    for s in declared_symbols():
+        assert hasattr(lib, s), s
+    assert _lib.load_debug() is not _lib.load()

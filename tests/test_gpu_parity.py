@@ -113,14 +113,19 @@ FRAME = {"cfg1_literal": 128, "cfg1_winaux": 128, "cfg2_literal": 128, "cfg2_win
          "frame512_same": 512, "frame64": 64, "frame64_same": 64}
 
 
-@pytest.fixture(params=[1, 2], ids=["cta", "cluster2"])
+@pytest.fixture(params=[(1, 0), (2, 0), (2, 1)], ids=["cta", "cluster2", "cluster2-staged-spectra"])
 def cluster_mode(request, cuda):
-    """Run a test with one CTA per patch, then with a 2-CTA cluster."""
+    """Run a test with one CTA per patch, then with a 2-CTA cluster; in the
+    last run kernels that multiply by cached spectra stage them in shared
+    memory by bulk copies (where they fit)."""
     from vmbd_gb300 import _lib
     lib = _lib.load()
-    _lib.check(lib.eff_set_cluster_mode(request.param))
-    yield request.param
+    mode, staging = request.param
+    _lib.check(lib.eff_set_cluster_mode(mode))
+    _lib.check(lib.eff_set_spectrum_staging(staging))
+    yield mode
     _lib.check(lib.eff_set_cluster_mode(0))
+    _lib.check(lib.eff_set_spectrum_staging(0))
 
 
 @pytest.mark.parametrize("name", list(CASES))
@@ -174,6 +179,7 @@ def test_operator_matches_fp64_oracle(cuda, cluster_mode, name):
         gx, gf = plan.adjoint(t(r, cuda), fh, xh, adjoint="reference")
         assert rel(gx.cpu().numpy(), eff64.adjoint_image(r, f, g, ws, exact=False)) < TOL
         assert rel(gf.cpu().numpy(), eff64.adjoint_psf(r, x, g, ws, exact=False)) < TOL
+    assert plan.device_errors() == 0
 
 
 def test_2048_stress_workload(cuda):

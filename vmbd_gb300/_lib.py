@@ -22,6 +22,7 @@ OUT_ZEROED = 1
 LOSS_OF_Y = 2
 OPERAND_IMAGE = 0
 OPERAND_PSF = 1
+GEOM_DETERMINISTIC = 1
 PROJ_CLIP_NORMALIZE = 0
 PROJ_SIMPLEX = 1
 
@@ -36,14 +37,14 @@ EXPORTS = (
     "eff_set_cluster_mode", "eff_batch_create", "eff_batch_destroy", "eff_batch_items",
     "eff_batch_forward_both", "eff_batch_adjoint_residual", "eff_deconv_xdirect", "eff_forward_ex",
     "eff_adjoint_ex", "eff_forward_residual", "eff_batch_forward_residual", "eff_test_plan_set_device",
-    "eff_forward_both_ex",
+    "eff_forward_both_ex", "eff_plan_device_errors", "eff_set_spectrum_staging",
 )
 
 
 class EffGeom(ctypes.Structure):
     _fields_ = [("sx", ctypes.c_int * 2), ("sf", ctypes.c_int * 2), ("csf", ctypes.c_int * 2),
                 ("sw", ctypes.c_int * 2), ("hop", ctypes.c_int * 2), ("sfft", ctypes.c_int),
-                ("mode", ctypes.c_int), ("threads", ctypes.c_int)]
+                ("mode", ctypes.c_int), ("threads", ctypes.c_int), ("flags", ctypes.c_int)]
 
 
 class EffError(RuntimeError):
@@ -53,6 +54,7 @@ class EffError(RuntimeError):
 
 
 _LIB = None
+_DEBUG_LIB = None
 
 
 def lib_path() -> str:
@@ -68,7 +70,27 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         _build.build()
     if not os.path.exists(_build.LIB):
         raise RuntimeError(f"{_build.LIB} is missing: run vmbd_gb300.build.build()")
-    L = ctypes.CDLL(_build.LIB)
+    _LIB = _bind(ctypes.CDLL(_build.LIB))
+    return _LIB
+
+
+def load_debug(build_if_missing: bool = True) -> ctypes.CDLL:
+    """The bounds-checked variant (frames 64 and 128; see vmbd_gb300.build):
+    the same C ABI, for tests that run small cases through it and then read
+    the plan's device error word."""
+    global _DEBUG_LIB
+    if _DEBUG_LIB is not None:
+        return _DEBUG_LIB
+    if build_if_missing and not _build.up_to_date(debug=True):
+        _build.build(debug=True)
+    if not os.path.exists(_build.DEBUG_LIB):
+        raise RuntimeError(f"{_build.DEBUG_LIB} is missing: run vmbd_gb300.build.build(debug=True)")
+    _DEBUG_LIB = _bind(ctypes.CDLL(_build.DEBUG_LIB))
+    return _DEBUG_LIB
+
+
+def _bind(L: ctypes.CDLL) -> ctypes.CDLL:
+    """Set the argument and result types of every exported entry point."""
     vp, ip, fp = ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p
     sig = {
         "eff_plan_create": ([ctypes.POINTER(EffGeom), fp, fp, ctypes.POINTER(vp)], ip),
@@ -96,6 +118,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "eff_max_nonneg": ([fp, ctypes.c_longlong, vp, vp], ip),
         "eff_set_cluster_mode": ([ip], ip),
         "eff_test_plan_set_device": ([vp, ip], ip),
+        "eff_plan_device_errors": ([vp, ctypes.POINTER(ctypes.c_int), ip], ip),
+        "eff_set_spectrum_staging": ([ip], ip),
         "eff_batch_create": ([vp, vp, ip, ctypes.POINTER(vp)], ip),
         "eff_batch_destroy": ([vp], ip),
         "eff_batch_items": ([vp], ip),
@@ -114,7 +138,6 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         fn = getattr(L, name)
         fn.argtypes = args
         fn.restype = res
-    _LIB = L
     return L
 
 

@@ -121,6 +121,8 @@ int eff_batch_create(const EffPlan* const* plans, const int* counts, int n_class
   for (int c = 0; c < n_classes; ++c) {
     if (!plans[c] || counts[c] < 1) return fail(EFF_ERR_INVALID, "bad plan or count");
     if (int s = eff::check_plan_device(plans[c])) return s;
+    if (eff::plan_deterministic(plans[c]))  // the persistent kernel overlap-adds with atomics
+      return fail(EFF_ERR_UNSUPPORTED, "deterministic plans are not supported in a persistent batch");
     B.plans[c] = plans[c];
     B.counts[c] = counts[c];
     int n = 0;

@@ -16,6 +16,7 @@
 
 #include "eff_internal.h"
 #include "eff_launch.cuh"
+#include "eff_ola.h"
 #include "../../include/vmbd_eff.h"
 
 namespace eff {
@@ -50,6 +51,10 @@ struct EffPlan {
   float2* win1;
   float2* tw;   // twiddle table [N], followed in the same allocation by
   float* lap;   // the difference-filter spectrum 4 sin^2(pi k / N) [N]
+  int* err;     // and the device error word
+  bool det;            // EFF_GEOM_DETERMINISTIC: tile stores + ola_gather instead of atomics
+  float* tiles;        // deterministic: one image's patch tiles, K * max(E0 E1, sw0 sw1) floats
+  double* loss_part;   // deterministic: one image's per-CTA loss shares, K * 8 doubles
 };
 
 namespace {
@@ -58,6 +63,10 @@ thread_local std::string g_last_error;
 constexpr size_t kSmemLimit = 227u * 1024u;
 // 0: choose per call; 1: one CTA per patch; 2: a 2-CTA cluster per patch.
 std::atomic<int> g_cluster_mode{0};
+// 1: stage cached spectra in shared memory where they fit; 0 (default): read
+// them from global memory (L2-resident in a step; measured faster on the
+// 512^2 step: adjoint 19.4 vs 21.6 us).
+std::atomic<int> g_stage_spectra{0};
 
 int fail(int code, const std::string& msg) {
   g_last_error = msg;
@@ -93,6 +102,7 @@ eff::Params base_params(const EffPlan* p) {
   P.win1 = p->win1;
   P.tw = p->tw;
   P.lap = p->lap;
+  P.err = p->err;
   P.x_bs = (long long)g.sx[0] * g.sx[1];
   P.f_bs = (long long)p->K * g.sf[0] * g.sf[1];
   P.y_bs = (long long)p->sy[0] * p->sy[1];
@@ -100,7 +110,109 @@ eff::Params base_params(const EffPlan* p) {
   return P;
 }
 
-int run(const EffPlan* p, int op, const eff::Params& P, int batch, void* stream) {
+int launch_kernel(const EffPlan* p, int op, const eff::Params& P, int batch, int CL, int threads, size_t smem,
+                  cudaStream_t st) {
+  cudaError_t e;
+  switch (p->N) {
+    case 64: e = eff::launch_n64(op, CL, P, p->K, batch, threads, smem, st); break;
+    case 128: e = eff::launch_n128(op, CL, P, p->K, batch, threads, smem, st); break;
+    case 192: e = eff::launch_n192(op, CL, P, p->K, batch, threads, smem, st); break;
+    case 256: e = eff::launch_n256(op, CL, P, p->K, batch, threads, smem, st); break;
+    case 512: e = eff::launch_n512(op, CL, P, p->K, batch, threads, smem, st); break;
+    default: return fail(EFF_ERR_UNSUPPORTED, "frame size");
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
+  return EFF_OK;
+}
+
+// Calls whose output is overlap-added (forwards; the image adjoint and the
+// loss; the deconvolution's image estimate) run, on a deterministic plan, as
+// the kernel storing patch tiles + ola_gather.
+bool deterministic_ola(const EffPlan* p, int op, const eff::Params& P) {
+  if (!p->det) return false;
+  if (op == eff::OP_FWD_IMAGE || op == eff::OP_FWD_PSF || op == eff::OP_FWD_BOTH) return true;
+  if (op == eff::OP_ADJ) return P.out0 || P.loss;
+  if (op == eff::OP_DECONV) return P.out0;
+  return false;
+}
+
+// Clear an output the kernels accumulate into (a deterministic plan's
+// outputs are stored whole by the gather instead: nothing to clear).
+cudaError_t clear_output(const EffPlan* p, void* ptr, size_t bytes, cudaStream_t st) {
+  if (p->det) return cudaSuccess;
+  return cudaMemsetAsync(ptr, 0, bytes, st);
+}
+
+// The parameters of image b of a batch, for a launch over that image alone.
+eff::Params image_params(const eff::Params& P, long long b) {
+  eff::Params Q = P;
+  auto adv = [b](auto* ptr, long long stride) { return ptr ? ptr + b * stride : ptr; };
+  Q.x = adv(P.x, P.x_bs);
+  Q.f = adv(P.f, P.f_bs);
+  Q.y = adv(P.y, P.y_bs);
+  Q.y_obs = adv(P.y_obs, P.y_bs);
+  Q.mask = adv(P.mask, P.y_bs);
+  Q.sub = adv(P.sub, P.y_bs);
+  Q.b0 = adv(P.b0, P.spec_bs);
+  Q.b1 = adv(P.b1, P.spec_bs);
+  Q.a_out = adv(P.a_out, P.spec_bs);
+  Q.b_out = adv(P.b_out, P.spec_bs);
+  Q.out0 = adv(P.out0, P.out0_bs);
+  Q.out1 = adv(P.out1, P.out1_bs);
+  Q.loss = adv(P.loss, 1);
+  Q.pf = adv(P.pf, P.pf_bytes);
+  return Q;
+}
+
+// Deterministic overlap-add: per image (the plan holds one image's tiles),
+// the kernel storing its patch tiles, then the gather summing them in a
+// fixed order (and subtracting the observation / summing the loss shares).
+int run_deterministic(const EffPlan* p, int op, const eff::Params& P, int batch, int CL, int threads, size_t smem,
+                      cudaStream_t st) {
+  const bool fwd = op == eff::OP_FWD_IMAGE || op == eff::OP_FWD_PSF || op == eff::OP_FWD_BOTH;
+  for (int b = 0; b < batch; ++b) {
+    eff::Params Q = image_params(P, b);
+    const float* sub = Q.sub;
+    Q.sub = nullptr;  // the gather subtracts it
+    Q.tiles = p->tiles;
+    Q.loss_part = (op == eff::OP_ADJ && Q.loss) ? p->loss_part : nullptr;
+    if (int s = launch_kernel(p, op, Q, 1, CL, threads, smem, st)) return s;
+    eff::GatherArgs A;
+    std::memset(&A, 0, sizeof(A));
+    A.tiles = p->tiles;
+    A.csf0 = p->g.csf[0];
+    A.csf1 = p->g.csf[1];
+    A.hop0 = p->g.hop[0];
+    A.hop1 = p->g.hop[1];
+    if (fwd) {
+      A.th = p->E[0];
+      A.tw = p->E[1];
+      A.off0 = p->off[0];
+      A.off1 = p->off[1];
+      A.rows = p->sy[0];
+      A.cols = p->sy[1];
+      A.sub = sub;
+    } else {
+      A.th = p->g.sw[0];
+      A.tw = p->g.sw[1];
+      A.rows = Q.out0 ? p->g.sx[0] : 0;
+      A.cols = Q.out0 ? p->g.sx[1] : 0;
+    }
+    A.out = Q.out0;
+    if (Q.loss_part) {
+      A.loss_part = Q.loss_part;
+      A.nparts = p->K * CL;
+      A.loss = Q.loss;
+    }
+    cudaError_t e = eff::launch_ola_gather(A, p->num_sms, st);
+    if (e != cudaSuccess) return cuda_fail(e, "overlap-add gather launch");
+  }
+  return EFF_OK;
+}
+
+int run(const EffPlan* p, int op, const eff::Params& P0, int batch, void* stream) {
+  eff::Params P = P0;
+  P.stage_spec = 0;
   const size_t smem1 = eff::smem_bytes(p->N, op, P, p->threads, 1);
   const size_t smem2 = eff::smem_bytes(p->N, op, P, p->threads2, 2);
   // A 2-CTA cluster per patch when one CTA's frame does not fit, or when the
@@ -113,22 +225,19 @@ int run(const EffPlan* p, int op, const eff::Params& P, int batch, void* stream)
   else if (mode == 1) CL = 1;
   else if (mode == 2) CL = 2;
   else CL = (2LL * p->K * batch <= p->num_sms) ? 2 : 1;
-  const size_t smem = CL == 1 ? smem1 : (CL == 2 ? smem2 : eff::smem_bytes(p->N, op, P, p->threads2, CL));
   const int threads = CL == 1 ? p->threads : p->threads2;
+  // Kernels that multiply by cached spectra stage their columns of them in
+  // shared memory where that still fits.
+  if (op == eff::OP_ADJ || op == eff::OP_FWD_IMAGE || op == eff::OP_FWD_PSF || op == eff::OP_DECONV) {
+    P.stage_spec = 1;
+    if (eff::smem_bytes(p->N, op, P, threads, CL) > kSmemLimit || !g_stage_spectra.load()) P.stage_spec = 0;
+  }
+  const size_t smem = eff::smem_bytes(p->N, op, P, threads, CL);
   if (smem > kSmemLimit)
     return fail(EFF_ERR_UNSUPPORTED, "frame needs " + std::to_string(smem) + " bytes of shared memory");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  cudaError_t e;
-  switch (p->N) {
-    case 64: e = eff::launch_n64(op, CL, P, p->K, batch, threads, smem, st); break;
-    case 128: e = eff::launch_n128(op, CL, P, p->K, batch, threads, smem, st); break;
-    case 192: e = eff::launch_n192(op, CL, P, p->K, batch, threads, smem, st); break;
-    case 256: e = eff::launch_n256(op, CL, P, p->K, batch, threads, smem, st); break;
-    case 512: e = eff::launch_n512(op, CL, P, p->K, batch, threads, smem, st); break;
-    default: return fail(EFF_ERR_UNSUPPORTED, "frame size");
-  }
-  if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
-  return EFF_OK;
+  if (deterministic_ola(p, op, P)) return run_deterministic(p, op, P, batch, CL, threads, smem, st);
+  return launch_kernel(p, op, P, batch, CL, threads, smem, st);
 }
 
 // The plan's tables live on the device that was current at eff_plan_create;
@@ -183,12 +292,12 @@ int adjoint_impl(const EffPlan* plan, const float* y, const float* y_obs, const 
   }
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   if (gx && !zeroed) {
-    cudaError_t e = cudaMemsetAsync(gx, 0, sizeof(float) * P.x_bs * batch, st);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+    cudaError_t e = clear_output(plan, gx, sizeof(float) * P.x_bs * batch, st);
+    if (e != cudaSuccess) return cuda_fail(e, "clearing an output");
   }
   if (loss && !zeroed) {
-    cudaError_t e = cudaMemsetAsync(loss, 0, sizeof(double) * batch, st);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+    cudaError_t e = clear_output(plan, loss, sizeof(double) * batch, st);
+    if (e != cudaSuccess) return cuda_fail(e, "clearing an output");
   }
   return run(plan, eff::OP_ADJ, P, batch, stream);
 }
@@ -240,8 +349,8 @@ int loss_grad_impl(const EffPlan* plan, const float* x, const float* f, const fl
   P.zero_nf = gx ? P.x_bs * batch : 0;
   P.zero_d = loss;
   P.zero_nd = loss ? batch : 0;
-  cudaError_t e = cudaMemsetAsync(y, 0, sizeof(float) * P.y_bs * batch, static_cast<cudaStream_t>(stream));
-  if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+  cudaError_t e = clear_output(plan, y, sizeof(float) * P.y_bs * batch, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "clearing an output");
   int s = run(plan, eff::OP_FWD_BOTH, P, batch, stream);
   if (s != EFF_OK) return s;
   return adjoint_impl(plan, y, nullptr, gx ? fhat : nullptr, gf ? xhat : nullptr, gx, gf, loss,
@@ -263,6 +372,8 @@ int eff::plan_patches(const EffPlan* plan) { return plan ? plan->K : 0; }
 
 int eff::plan_device(const EffPlan* plan) { return plan ? plan->device : -1; }
 
+bool eff::plan_deterministic(const EffPlan* plan) { return plan && plan->det; }
+
 int eff::check_plan_device(const EffPlan* plan) {
   if (!plan) return fail(EFF_ERR_INVALID, "null plan");
   return check_device(plan);
@@ -283,12 +394,14 @@ int eff_plan_create(const EffGeom* geom, const float* win0, const float* win1, E
       return fail(EFF_ERR_INVALID, "Size missmatch: PSF must be smaller than the image");
   }
   if (g.mode < EFF_MODE_VALID || g.mode > EFF_MODE_FULL) return fail(EFF_ERR_INVALID, "Not a valid mode!");
+  if (g.flags & ~EFF_GEOM_DETERMINISTIC) return fail(EFF_ERR_INVALID, "unknown geometry flags");
   if ((long long)g.csf[0] * g.csf[1] > 65535) return fail(EFF_ERR_UNSUPPORTED, "too many patches");
 
   EffPlan p;
   std::memset(&p, 0, sizeof(p));
   p.g = g;
   p.K = g.csf[0] * g.csf[1];
+  p.det = (g.flags & EFF_GEOM_DETERMINISTIC) != 0;
   for (int d = 0; d < 2; ++d) {
     p.E[d] = g.sw[d] + g.sf[d] - 1;
     if (g.mode == EFF_MODE_VALID) { p.sy[d] = g.sx[d] - g.sf[d] + 1; p.off[d] = g.sf[d] - 1; }
@@ -399,9 +512,14 @@ int eff_plan_create(const EffGeom* geom, const float* win0, const float* win1, E
     lap[k] = (float)(4.0 * s * s);
   }
   const size_t n0 = 2 * (size_t)g.csf[0] * g.sw[0], n1 = 2 * (size_t)g.csf[1] * g.sw[1];
-  if ((e = cudaMalloc(&p.tw, (sizeof(float2) + sizeof(float)) * p.N)) != cudaSuccess)
+  if ((e = cudaMalloc(&p.tw, (sizeof(float2) + sizeof(float)) * p.N + sizeof(int))) != cudaSuccess)
     return cuda_fail(e, "cudaMalloc");
   p.lap = reinterpret_cast<float*>(p.tw + p.N);
+  p.err = reinterpret_cast<int*>(p.lap + p.N);
+  if ((e = cudaMemset(p.err, 0, sizeof(int))) != cudaSuccess) {
+    cudaFree(p.tw);
+    return cuda_fail(e, "cudaMemset");
+  }
   if ((e = cudaMalloc(&p.win0, sizeof(float) * n0)) != cudaSuccess) {
     cudaFree(p.tw);
     return cuda_fail(e, "cudaMalloc");
@@ -420,8 +538,21 @@ int eff_plan_create(const EffGeom* geom, const float* win0, const float* win1, E
     cudaFree(p.win1);
     return cuda_fail(e, "cudaMemcpy");
   }
+  if (p.det) {
+    const size_t tile = std::max((size_t)p.E[0] * p.E[1], (size_t)g.sw[0] * g.sw[1]);
+    if ((e = cudaMalloc(&p.tiles, sizeof(float) * p.K * tile)) != cudaSuccess ||
+        (e = cudaMalloc(&p.loss_part, sizeof(double) * p.K * 8)) != cudaSuccess) {
+      cudaFree(p.tiles);
+      cudaFree(p.tw);
+      cudaFree(p.win0);
+      cudaFree(p.win1);
+      return cuda_fail(e, "cudaMalloc");
+    }
+  }
   EffPlan* out = new (std::nothrow) EffPlan(p);
   if (!out) {
+    cudaFree(p.tiles);
+    cudaFree(p.loss_part);
     cudaFree(p.tw);
     cudaFree(p.win0);
     cudaFree(p.win1);
@@ -436,6 +567,8 @@ int eff_plan_destroy(EffPlan* plan) {
   cudaFree(plan->tw);
   cudaFree(plan->win0);
   cudaFree(plan->win1);
+  cudaFree(plan->tiles);
+  cudaFree(plan->loss_part);
   delete plan;
   return EFF_OK;
 }
@@ -479,8 +612,8 @@ int eff_forward_image(const EffPlan* plan, const float* x, const void* fhat, flo
   P.out0 = y;
   P.out0_bs = P.y_bs;
   P.a_out = static_cast<float2*>(xhat_out);
-  cudaError_t e = cudaMemsetAsync(y, 0, sizeof(float) * P.y_bs * batch, static_cast<cudaStream_t>(stream));
-  if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+  cudaError_t e = clear_output(plan, y, sizeof(float) * P.y_bs * batch, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "clearing an output");
   return run(plan, eff::OP_FWD_IMAGE, P, batch, stream);
 }
 
@@ -494,8 +627,8 @@ int eff_forward_psf(const EffPlan* plan, const float* f, const void* xhat, float
   P.out0 = y;
   P.out0_bs = P.y_bs;
   P.a_out = static_cast<float2*>(fhat_out);
-  cudaError_t e = cudaMemsetAsync(y, 0, sizeof(float) * P.y_bs * batch, static_cast<cudaStream_t>(stream));
-  if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+  cudaError_t e = clear_output(plan, y, sizeof(float) * P.y_bs * batch, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "clearing an output");
   return run(plan, eff::OP_FWD_PSF, P, batch, stream);
 }
 
@@ -521,8 +654,8 @@ int eff_forward_ex(const EffPlan* plan, int operand, const float* u, const void*
   P.zero_d = zero_nd > 0 ? zero_d : nullptr;
   P.zero_nd = zero_nd;
   if (!(flags & EFF_OUT_ZEROED)) {
-    cudaError_t e = cudaMemsetAsync(y, 0, sizeof(float) * P.y_bs * batch, static_cast<cudaStream_t>(stream));
-    if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+    cudaError_t e = clear_output(plan, y, sizeof(float) * P.y_bs * batch, static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "clearing an output");
   }
   return run(plan, operand == EFF_OPERAND_IMAGE ? eff::OP_FWD_IMAGE : eff::OP_FWD_PSF, P, batch, stream);
 }
@@ -573,8 +706,8 @@ int eff_deconv_xdirect(const EffPlan* plan, const float* y, const void* fhat, co
   P.beta = beta;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   if (u) {
-    cudaError_t e = cudaMemsetAsync(u, 0, sizeof(float) * P.x_bs * batch, st);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+    cudaError_t e = clear_output(plan, u, sizeof(float) * P.x_bs * batch, st);
+    if (e != cudaSuccess) return cuda_fail(e, "clearing an output");
   }
   return run(plan, eff::OP_DECONV, P, batch, stream);
 }
@@ -596,8 +729,8 @@ int eff_forward_both(const EffPlan* plan, const float* x, const float* f, float*
   P.out0_bs = P.y_bs;
   P.a_out = static_cast<float2*>(xhat_out);
   P.b_out = static_cast<float2*>(fhat_out);
-  cudaError_t e = cudaMemsetAsync(y, 0, sizeof(float) * P.y_bs * batch, static_cast<cudaStream_t>(stream));
-  if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+  cudaError_t e = clear_output(plan, y, sizeof(float) * P.y_bs * batch, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "clearing an output");
   return run(plan, eff::OP_FWD_BOTH, P, batch, stream);
 }
 
@@ -616,8 +749,8 @@ int eff_forward_residual(const EffPlan* plan, const float* x, const float* f, co
   P.pf = reinterpret_cast<const char*>(y_obs);
   P.pf_bytes = (long long)sizeof(float) * P.y_bs;
   P.sub = y_obs;
-  cudaError_t e = cudaMemsetAsync(r, 0, sizeof(float) * P.y_bs * batch, static_cast<cudaStream_t>(stream));
-  if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+  cudaError_t e = clear_output(plan, r, sizeof(float) * P.y_bs * batch, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "clearing an output");
   return run(plan, eff::OP_FWD_BOTH, P, batch, stream);
 }
 
@@ -646,8 +779,8 @@ int eff_forward_both_ex(const EffPlan* plan, const float* x, const float* f, con
   P.zero_d = zero_nd > 0 ? zero_d : nullptr;
   P.zero_nd = zero_nd;
   if (!(flags & EFF_OUT_ZEROED)) {
-    cudaError_t e = cudaMemsetAsync(y, 0, sizeof(float) * P.y_bs * batch, static_cast<cudaStream_t>(stream));
-    if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+    cudaError_t e = clear_output(plan, y, sizeof(float) * P.y_bs * batch, static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "clearing an output");
   }
   return run(plan, eff::OP_FWD_BOTH, P, batch, stream);
 }
@@ -732,6 +865,22 @@ int eff_mu_update(float* x, const float* num, const float* den, float tol, int r
                                         floor_rel, xmax_bits, (flags & EFF_OUT_ZEROED) != 0, zero_f, zero_n,
                                         static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(e, "mu_update launch");
+  return EFF_OK;
+}
+
+int eff_plan_device_errors(const EffPlan* plan, int* flags, int clear) {
+  if (!plan || !flags) return fail(EFF_ERR_INVALID, "null argument");
+  if (int s = check_device(plan)) return s;
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(flags, plan->err, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && clear) e = cudaMemset(plan->err, 0, sizeof(int));
+  if (e != cudaSuccess) return cuda_fail(e, "reading the device error word");
+  return EFF_OK;
+}
+
+int eff_set_spectrum_staging(int on) {
+  if (on != 0 && on != 1) return fail(EFF_ERR_INVALID, "spectrum staging must be 0 or 1");
+  g_stage_spectra.store(on);
   return EFF_OK;
 }
 

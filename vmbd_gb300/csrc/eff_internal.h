@@ -12,4 +12,6 @@ int plan_device(const EffPlan* plan);
 // EFF_OK when the plan's device is the current device, else an
 // EFF_ERR_INVALID / EFF_ERR_CUDA status with the message recorded.
 int check_plan_device(const EffPlan* plan);
+// The plan was created with EFF_GEOM_DETERMINISTIC.
+bool plan_deterministic(const EffPlan* plan);
 }  // namespace eff

@@ -77,6 +77,14 @@ struct Params {
   const float* sub;        // forward: subtract this plane [sy0, sy1] from out0 too (a share per CTA, by
                            //   atomics), so that out0 ends as EFF(...) - sub
   int loss_y;              // adjoint without y_obs: loss += 0.5 * sum y^2 (y is already the residual)
+  int stage_spec;          // eff_kernel: copy this CTA's columns of the cached spectra into shared
+                           //   memory (cp.async.bulk) at kernel start (host: only where they fit)
+  int* err;                // device error word of the plan (bit 0: a bulk copy did not complete in time)
+  float* tiles;            // deterministic overlap-add: the forward stores patch k's E0 x E1 output tile
+                           //   (the image adjoint / deconvolution its sw0 x sw1 tile) at
+                           //   tiles + (b K + k) * tile size, instead of adding it into the image;
+                           //   ola_gather sums the tiles in a fixed order
+  double* loss_part;       // deterministic loss: each CTA stores its share at loss_part[b ncta + cta]
 };
 
 // TMA bulk prefetch of a contiguous range into L2 (16-byte aligned start and
@@ -84,6 +92,59 @@ struct Params {
 __device__ __forceinline__ void l2_prefetch_bulk(const void* p, unsigned bytes) {
   asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
 }
+
+// --- bulk copies into shared memory, completed on an mbarrier -------------
+__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+}
+// Contiguous global -> this CTA's shared memory (16-byte aligned, size a
+// multiple of 16), counted on bar.
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_addr(dst)),
+               "l"(src), "r"(bytes), "r"(smem_addr(bar))
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Wait for phase `parity` of bar with an iteration limit (each try_wait may
+// suspend the thread for a while): false when the limit ran out.
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity) {
+  for (int i = 0; i < (1 << 22); ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+constexpr int kErrCopyTimeout = 1;
+constexpr int kErrBounds = 2;
+
+// Debug builds (-DEFF_DEBUG, the library's checked variant): every frame and
+// global index the kernels form is tested against its buffer before the
+// access; a bad index sets kErrBounds in the plan's device error word and
+// the access is skipped, so the kernel runs to its end and the host can read
+// the error.  In the product build EFF_IN is the constant true.
+#ifdef EFF_DEBUG
+__device__ __forceinline__ bool dbg_in(long long i, long long n, int* err) {
+  if (i >= 0 && i < n) return true;
+  if (err) atomicOr(err, kErrBounds);
+  return false;
+}
+#define EFF_IN(i, n, err) ::eff::dbg_in((long long)(i), (long long)(n), (err))
+#else
+#define EFF_IN(i, n, err) true
+#endif
 
 // Half-spectrum bins a CTA stores per row: all N/2+1 (CL = 1) or its
 // quarter plus, on CTA 0, the N/2 bin (CL = 2).
@@ -117,6 +178,19 @@ __host__ __device__ inline int frame_rows(const Params& P, int op) {
   return max(ra, r0 + r1);
 }
 
+// Cached spectra staged in shared memory: how many (in order b0, b1), the
+// columns a CTA keeps of each (its W bins plus a slot for bin N/2, used on
+// CTA 0), and the padding per column (spreads the four lane groups of a
+// warp, which read four neighbouring columns, over the banks).
+constexpr int kSpecPad = 8;
+__host__ __device__ inline int staged_specs(const Params& P, int op) {
+  if (!P.stage_spec) return 0;
+  if (op == OP_FWD_IMAGE || op == OP_FWD_PSF) return 1;
+  if (op == OP_ADJ || op == OP_DECONV) return (P.out0 ? 1 : 0) + (P.out1 ? 1 : 0);
+  return 0;
+}
+__host__ __device__ constexpr int staged_cols(int N, int CL) { return N / (2 * CL) + 1; }
+
 template <int N>
 __device__ __forceinline__ unsigned group_mask(int lane) {
   constexpr int G = FftShape<N>::G;
@@ -133,6 +207,8 @@ struct Frame {
   float2* part[CL];  // generic pointers to every CTA's frame (own one included)
   float2* local;     // this CTA's frame (shared window)
   int rank;
+  int rows;          // frame rows of every CTA (bound of the debug build's checks)
+  int* err;          // plan's device error word (debug build)
   // Owner and local column of half-spectrum bin b.
   __device__ __forceinline__ static int owner(int b) { return (CL == 1 || b == N / 2) ? 0 : b / W; }
   __device__ __forceinline__ static int lcol(int b) {
@@ -169,7 +245,9 @@ __device__ __forceinline__ float operand(const Params& P, const Patch& T, int r,
   static_assert(KIND == OPND_PSF || KIND == OPND_DCHOP, "image / residual rows: load_image_rows / load_resid_rows");
   if constexpr (KIND == OPND_PSF) {
     if (r >= P.sf0 || c >= P.sf1) return 0.f;
-    return __ldg(T.f + ((long long)T.k * P.sf0 + r) * P.sf1 + c);
+    const long long q = ((long long)T.k * P.sf0 + r) * P.sf1 + c;
+    if (!EFF_IN(q, (long long)P.csf0 * P.csf1 * P.sf0 * P.sf1, P.err)) return 0.f;
+    return __ldg(T.f + q);
   } else {
     // deconv 'xdirect': chop of y placed at frame offset lo (chop_pad_GPU,
     // olaGPU.py:573-580) times the window stack at the frame origin
@@ -177,6 +255,9 @@ __device__ __forceinline__ float operand(const Params& P, const Patch& T, int r,
     if (r < P.lo0 || r >= P.sw0 || c < P.lo1 || c >= P.sw1) return 0.f;
     const int i = T.m * P.hop0 + r - P.lo0, j = T.n * P.hop1 + c - P.lo1;
     if (i >= P.sy0 || j >= P.sy1) return 0.f;
+    if (!EFF_IN((long long)i * P.sy1 + j, (long long)P.sy0 * P.sy1, P.err) ||
+        !EFF_IN(T.m * P.sw0 + r, P.csf0 * P.sw0, P.err) || !EFF_IN(T.n * P.sw1 + c, P.csf1 * P.sw1, P.err))
+      return 0.f;
     return window_weight(__ldg(P.win0 + T.m * P.sw0 + r), __ldg(P.win1 + T.n * P.sw1 + c)) *
            __ldg(T.y + (long long)i * P.sy1 + j);
   }
@@ -202,7 +283,8 @@ __device__ __forceinline__ void load_resid_rows(const Params& P, const Patch& T,
 #pragma unroll
   for (int mm = 0; mm < R; ++mm) {
     const int c = g + G * mm;
-    const bool cv = c >= clo && c < chi;
+    const bool cv = c >= clo && c < chi && (!okA || EFF_IN(oa + c, (long long)P.sy0 * P.sy1, P.err)) &&
+                    (!okB || EFF_IN(ob + c, (long long)P.sy0 * P.sy1, P.err));
     float a = 0.f, b = 0.f;
     if (cv && okA) {
       a = __ldg(T.y + (oa + c));
@@ -230,8 +312,9 @@ __device__ __forceinline__ void load_image_rows(const Params& P, const Patch& T,
   const int i0 = T.m * P.hop0 + ra;
   const bool okA = ra < P.sw0 && i0 < P.sx0;
   const bool okB = ra + 1 < P.sw0 && i0 + 1 < P.sx0;
-  const float2 wa = okA ? __ldg(P.win0 + T.m * P.sw0 + ra) : make_float2(0.f, 0.f);
-  const float2 wb = okB ? __ldg(P.win0 + T.m * P.sw0 + ra + 1) : make_float2(0.f, 0.f);
+  const bool okW = !(okA || okB) || EFF_IN(T.m * P.sw0 + ra + (okB ? 1 : 0), P.csf0 * P.sw0, P.err);
+  const float2 wa = okA && okW ? __ldg(P.win0 + T.m * P.sw0 + ra) : make_float2(0.f, 0.f);
+  const float2 wb = okB && okW ? __ldg(P.win0 + T.m * P.sw0 + ra + 1) : make_float2(0.f, 0.f);
   const int jb = T.n * P.hop1;
   const int chi = min(P.sw1, P.sx1 - jb);
   const long long oa = (long long)i0 * P.sx1 + jb, ob = oa + P.sx1;
@@ -240,7 +323,9 @@ __device__ __forceinline__ void load_image_rows(const Params& P, const Patch& T,
   for (int mm = 0; mm < R; ++mm) {
     const int c = g + G * mm;
     float a = 0.f, b = 0.f;
-    if (c < chi) {
+    if (c < chi && EFF_IN(T.n * P.sw1 + c, P.csf1 * P.sw1, P.err) &&
+        (!okA || EFF_IN(oa + c, (long long)P.sx0 * P.sx1, P.err)) &&
+        (!okB || EFF_IN(ob + c, (long long)P.sx0 * P.sx1, P.err))) {
       const float2 wc = __ldg(w1 + c);
       if (okA) a = window_weight(wa, wc) * __ldg(T.x + (oa + c));
       if (okB) b = window_weight(wb, wc) * __ldg(T.x + (ob + c));
@@ -271,17 +356,24 @@ __device__ __forceinline__ void load_rows(const Params& P, const Patch& T, int r
   }
 }
 
-// R2C of one pair of rows already in v (layout A) into frame rows row,
-// row+1 (bins go to the CTA that owns their column).
+// R2C of one pair of rows already in v (layout A), first half: the packed
+// transform in v and its Hermitian partners in p (registers only, no frame
+// access, so it may run before the cluster's CTAs are known to be running).
+template <int N>
+__device__ __forceinline__ void r2c_transform(float2 (&v)[FftShape<N>::R], float2 (&p)[FftShape<N>::R], float2* scr,
+                                              const float2* tw, int g, unsigned gmask) {
+  fft_fwd<N>(v, g, scr, tw, gmask);
+  hermitian_partner<N>(v, p, g, gmask);
+}
+
+// Second half: the two half-spectrum rows split from (v, p) into frame rows
+// row, row+1 (bins go to the CTA that owns their column).
 template <int N, int CL>
-__device__ __forceinline__ void r2c_store(float2 (&v)[FftShape<N>::R], const Frame<N, CL>& F, int row, float2* scr,
-                                          const float2* tw, int g, unsigned gmask) {
+__device__ __forceinline__ void r2c_scatter(const float2 (&v)[FftShape<N>::R], const float2 (&p)[FftShape<N>::R],
+                                            const Frame<N, CL>& F, int row, int g) {
   constexpr int G = FftShape<N>::G;
   constexpr int R = FftShape<N>::R;
   constexpr int HP = Frame<N, CL>::HP;
-  fft_fwd<N>(v, g, scr, tw, gmask);
-  float2 p[R];
-  hermitian_partner<N>(v, p, g, gmask);
   // bins g + G*j of one CTA's range [c W, (c+1) W) are those with j / JW == c
   // (W is a multiple of G); the N/2 bin (j = R/2, lane 0) goes to CTA 0
   constexpr int W = Frame<N, CL>::W;
@@ -295,6 +387,7 @@ __device__ __forceinline__ void r2c_store(float2 (&v)[FftShape<N>::R], const Fra
     float2* base = F.part[own];
     const int col = CL == 1 ? kk : (j == R / 2 ? W : kk - own * W);
     float2* rowa = base + row * HP + col;
+    if (!EFF_IN((row + 1) * HP + col, F.rows * HP, F.err) || !EFF_IN(col, HP, F.err)) continue;
     rowa[0] = make_float2(0.5f * (v[j].x + p[j].x), 0.5f * (v[j].y - p[j].y));
     rowa[HP] = make_float2(0.5f * (v[j].y + p[j].y), 0.5f * (p[j].x - v[j].x));
   }
@@ -311,17 +404,17 @@ __device__ __forceinline__ void c2r_unit(const Frame<N, CL>& F, int ra, float2 (
 #pragma unroll
   for (int j = 0; j < R; ++j) {
     const int kk = g + G * j;
-    float2 ya, yb;
-    if (j < R / 2 || (j == R / 2 && g == 0)) {
-      const float2* pa = F.at(ra, kk);
+    float2 ya = make_float2(0.f, 0.f), yb = ya;
+    const bool lo = j < R / 2 || (j == R / 2 && g == 0);
+    const int bin = lo ? kk : N - kk;
+    if (EFF_IN((ra + 1) * HP + F.lcol(bin), F.rows * HP, F.err) && EFF_IN(F.lcol(bin), HP, F.err)) {
+      const float2* pa = F.at(ra, bin);
       ya = pa[0];
       yb = pa[HP];
-    } else {
-      const float2* pa = F.at(ra, N - kk);
-      ya = pa[0];
-      yb = pa[HP];
-      ya.y = -ya.y;
-      yb.y = -yb.y;
+      if (!lo) {
+        ya.y = -ya.y;
+        yb.y = -yb.y;
+      }
     }
     v[j] = make_float2(ya.x - yb.y, ya.y + yb.x);
   }
@@ -332,13 +425,13 @@ __device__ __forceinline__ void c2r_unit(const Frame<N, CL>& F, int ra, float2 (
 // [base, base+rows), frame pitch HP.
 template <int N, int HP>
 __device__ __forceinline__ void load_column(const float2* frame, int col, bool dc, int dcN, int base, int rows,
-                                            int g, float2 (&v)[FftShape<N>::R]) {
+                                            int g, float2 (&v)[FftShape<N>::R], int frows, int* err) {
   constexpr int G = FftShape<N>::G;
   constexpr int R = FftShape<N>::R;
 #pragma unroll
   for (int mm = 0; mm < R; ++mm) {
     const int r = g + G * mm;
-    if (r < rows) {
+    if (r < rows && EFF_IN(base + r, frows, err) && EFF_IN(dc ? dcN : col, HP, err)) {
       const float2* row = frame + (base + r) * HP;
       v[mm] = dc ? make_float2(row[0].x, row[dcN].x) : row[col];
     } else {
@@ -350,14 +443,14 @@ __device__ __forceinline__ void load_column(const float2* frame, int col, bool d
 // Inverse-transformed column to rows [base, base + even(rows)).
 template <int N, int HP>
 __device__ __forceinline__ void store_column(float2* frame, int col, bool dc, int dcN, int base, int rows,
-                                             int g, const float2 (&v)[FftShape<N>::R]) {
+                                             int g, const float2 (&v)[FftShape<N>::R], int frows, int* err) {
   constexpr int G = FftShape<N>::G;
   constexpr int R = FftShape<N>::R;
   const int rows_e = even_up(rows);
 #pragma unroll
   for (int mm = 0; mm < R; ++mm) {
     const int r = g + G * mm;
-    if (r < rows_e) {
+    if (r < rows_e && EFF_IN(base + r, frows, err) && EFF_IN(dc ? dcN : col, HP, err)) {
       float2* row = frame + (base + r) * HP;
       if (dc) {
         row[0] = make_float2(v[mm].x, 0.f);
@@ -392,9 +485,10 @@ __device__ __forceinline__ void dc_split(const float2 (&v)[FftShape<N>::R], floa
 // u != 0, the DC stash's two columns for u == 0.
 template <int N>
 __device__ __forceinline__ void store_spectrum(float2* __restrict__ dst, int u, int g,
-                                               const float2 (&a)[FftShape<N>::R], const float2* stash) {
+                                               const float2 (&a)[FftShape<N>::R], const float2* stash, int* err) {
   constexpr int G = FftShape<N>::G;
   constexpr int R = FftShape<N>::R;
+  if (!EFF_IN(u, N / 2, err)) return;  // bins 0 .. N/2 - 1 (bin N/2 with unit 0)
   float2* c0 = dst + (long long)u * N;
   if (u != 0) {
 #pragma unroll
@@ -412,25 +506,29 @@ __device__ __forceinline__ void store_spectrum(float2* __restrict__ dst, int u, 
 // Product of the column spectrum with a cached spectrum bh, packed for one
 // inverse transform: u != 0 from a; u == 0 from the DC stash, column 0
 // product + i * column N/2 product.  out may alias a.
+// Element i of a cached spectrum column, staged in shared memory or in
+// global memory (a generic load serves both, so one code path does).
+__device__ __forceinline__ float2 spec_at(const float2* c, int i) { return c[i]; }
+
+// c0: the cached spectrum's column of this unit's bin, cN: of bin N/2 (read
+// by the DC unit, u == 0, only).
 template <int N, bool CONJ>
 __device__ __forceinline__ void column_product(const float2 (&a)[FftShape<N>::R], const float2* stash,
-                                               const float2* __restrict__ bh, int u, int g,
+                                               const float2* c0, const float2* cN, int u, int g,
                                                float scale, float2 (&out)[FftShape<N>::R]) {
   constexpr int G = FftShape<N>::G;
   constexpr int R = FftShape<N>::R;
-  const float2* c0 = bh + (long long)u * N;
   if (u != 0) {
 #pragma unroll
     for (int j = 0; j < R; ++j) {
-      const float2 s = __ldg(c0 + g + G * j);
+      const float2 s = spec_at(c0, g + G * j);
       out[j] = cscale(CONJ ? cmulc(a[j], s) : cmul(a[j], s), scale);
     }
   } else {
-    const float2* cN = bh + (long long)(N / 2) * N;
 #pragma unroll
     for (int j = 0; j < R; ++j) {
-      const float2 s0 = __ldg(c0 + g + G * j);
-      const float2 sN = __ldg(cN + g + G * j);
+      const float2 s0 = spec_at(c0, g + G * j);
+      const float2 sN = spec_at(cN, g + G * j);
       const float2 p0 = CONJ ? cmulc(stash[j * G + g], s0) : cmul(stash[j * G + g], s0);
       const float2 pN = CONJ ? cmulc(stash[N + j * G + g], sN) : cmul(stash[N + j * G + g], sN);
       out[j] = make_float2((p0.x - pN.y) * scale, (p0.y + pN.x) * scale);
@@ -445,27 +543,25 @@ __device__ __forceinline__ void column_product(const float2 (&a)[FftShape<N>::R]
 // out may alias a.
 template <int N>
 __device__ __forceinline__ void column_divide(const float2 (&a)[FftShape<N>::R], const float2* stash,
-                                              const float2* __restrict__ bh, const float* __restrict__ lap,
+                                              const float2* c0, const float2* cN, const float* __restrict__ lap,
                                               int u, int g, float alpha, float beta, float scale,
                                               float2 (&out)[FftShape<N>::R]) {
   constexpr int G = FftShape<N>::G;
   constexpr int R = FftShape<N>::R;
-  const float2* c0 = bh + (long long)u * N;
   if (u != 0) {
     const float ru = fmaf(alpha, __ldg(lap + u), beta);
 #pragma unroll
     for (int j = 0; j < R; ++j) {
-      const float2 s = __ldg(c0 + g + G * j);
+      const float2 s = spec_at(c0, g + G * j);
       const float den = fmaf(s.x, s.x, s.y * s.y) + fmaf(alpha, __ldg(lap + g + G * j), ru);
       out[j] = cscale(cmulc(a[j], s), scale / den);
     }
   } else {
-    const float2* cN = bh + (long long)(N / 2) * N;
     const float r0 = fmaf(alpha, __ldg(lap), beta), rN = fmaf(alpha, __ldg(lap + N / 2), beta);
 #pragma unroll
     for (int j = 0; j < R; ++j) {
-      const float2 s0 = __ldg(c0 + g + G * j);
-      const float2 sN = __ldg(cN + g + G * j);
+      const float2 s0 = spec_at(c0, g + G * j);
+      const float2 sN = spec_at(cN, g + G * j);
       const float lk = alpha * __ldg(lap + g + G * j);
       const float d0 = fmaf(s0.x, s0.x, s0.y * s0.y) + (lk + r0);
       const float dN = fmaf(sN.x, sN.x, sN.y * sN.y) + (lk + rN);
@@ -523,6 +619,8 @@ __device__ __forceinline__ void eff_patch(const Params& P, int k, long long b, f
 
   Frame<N, CL> F;
   F.local = frame;
+  F.rows = frame_rows(P, OP);
+  F.err = P.err;
   if constexpr (CL == 1) {
     F.rank = 0;
     F.part[0] = frame;
@@ -559,8 +657,41 @@ __device__ __forceinline__ void eff_patch(const Params& P, int k, long long b, f
   const int baseB = even_up(rowsA);
   float2* scr = frame + frame_rows(P, OP) * HP + gid * FftShape<N>::SCR;
   float2* stash = frame + frame_rows(P, OP) * HP + NG * FftShape<N>::SCR;  // 2N, DC unit only
+  // Staged cached spectra: nst columns blocks of SC columns of N + kSpecPad,
+  // then the mbarrier their copies complete on.
+  constexpr int SC = staged_cols(N, CL);
+  constexpr int SP = N + kSpecPad;
+  const int nst = staged_specs(P, OP);
+  float2* stage = stash + 2 * N;
+  stage += (reinterpret_cast<unsigned long long>(stage) & 15ull) ? 1 : 0;
+  unsigned long long* sbar = reinterpret_cast<unsigned long long*>(stage + nst * SC * SP);
 
   for (int i = tid; i < N; i += blockDim.x) tw[i] = __ldg(P.tw + i);
+  if (nst && tid == 0) mbar_init(sbar, 1);
+  __syncthreads();  // the twiddles (and the mbarrier), before the first use
+  // Cached spectra this CTA multiplies by in the column pass: its columns of
+  // each, copied into shared memory by the bulk-copy engine while the row
+  // pass runs (one column per copy, into padded slots).
+  if (nst && tid < 32) {
+    const int c0 = CL == 1 ? 0 : F.rank * Frame<N, CL>::W;
+    const int ncol = CL == 1 ? N / 2 + 1 : Frame<N, CL>::W + (F.rank == 0 ? 1 : 0);
+    if (tid == 0) mbar_expect_tx(sbar, (unsigned)(nst * ncol * N * sizeof(float2)));
+    __syncwarp();
+    const float2* src[2];
+    int k = 0;
+    if (OP == OP_ADJ || OP == OP_DECONV) {
+      if (P.out0) src[k++] = b0;
+      if (P.out1) src[k++] = b1;
+    } else {
+      src[k++] = b0;
+    }
+    for (int q = tid; q < nst * ncol; q += 32) {
+      const int si = q / ncol, l = q - si * ncol;
+      // local slot l < W: bin c0 + l; slot W (CTA 0 of a cluster): bin N/2
+      const int bin = (CL > 1 && l == Frame<N, CL>::W) ? N / 2 : c0 + l;
+      bulk_copy_g2s(stage + (si * SC + l) * SP, src[si] + (long long)bin * N, N * sizeof(float2), sbar);
+    }
+  }
 
   // Fused forward of a loss/gradient step: start pulling the observation
   // the adjoint will read into L2 (this CTA's 16-byte-aligned share).
@@ -579,7 +710,7 @@ __device__ __forceinline__ void eff_patch(const Params& P, int k, long long b, f
   // columns this CTA owns into L2 now, so that a cold spectrum arrives while
   // the row pass runs (TMA bulk prefetch; a hint, the loads stay as they are).
   if constexpr (OP == OP_FWD_IMAGE || OP == OP_FWD_PSF || OP == OP_ADJ || OP == OP_DECONV) {
-    if (tid < 2) {
+    if (!nst && tid < 2) {
       const float2* sp = tid == 0 ? b0 : b1;
       if (sp && (reinterpret_cast<unsigned long long>(sp) & 15ull) == 0) {
         const int c0 = CL == 1 ? 0 : F.rank * Frame<N, CL>::W;
@@ -589,16 +720,13 @@ __device__ __forceinline__ void eff_patch(const Params& P, int k, long long b, f
       }
     }
   }
-  // The peer must not write into this CTA's frame before it is running (and,
-  // in a persistent loop, before this CTA has finished the previous patch).
-  phase_sync();
-
-  // Phase 1: row transforms of operand A (and B).
+  // Phase 1: row transforms of operand A (and B).  A lane group's first
+  // unit is loaded and transformed before the cluster barrier below, so its
+  // loads overlap the cluster's start; only its stores into the frames wait.
   {
     const int nA = (rowsA + 1) >> 1;
     const int nB = has_b(OP) ? (P.sf0 + 1) >> 1 : 0;
-    for (int u = wid; u < nA + nB; u += NW) {
-      float2 v[R];
+    auto transform_unit = [&](int u, float2 (&v)[R], float2 (&p)[R]) -> int {
       int row;
       if (u < nA) {
         load_rows<N, A>(P, T, 2 * u, g, v);
@@ -607,7 +735,19 @@ __device__ __forceinline__ void eff_patch(const Params& P, int k, long long b, f
         load_rows<N, OPND_PSF>(P, T, 2 * (u - nA), g, v);
         row = baseB + 2 * (u - nA);
       }
-      r2c_store<N, CL>(v, F, row, scr, tw, g, gmask);
+      r2c_transform<N>(v, p, scr, tw, g, gmask);
+      return row;
+    };
+    float2 v[R], p[R];
+    int row = -1;
+    if (wid < nA + nB) row = transform_unit(wid, v, p);
+    // The peer must not write into this CTA's frame before it is running (and,
+    // in a persistent loop, before this CTA has finished the previous patch).
+    phase_sync();
+    if (row >= 0) r2c_scatter<N, CL>(v, p, F, row, g);
+    for (int u = wid + NW; u < nA + nB; u += NW) {
+      row = transform_unit(u, v, p);
+      r2c_scatter<N, CL>(v, p, F, row, g);
     }
   }
   phase_sync();
@@ -622,40 +762,51 @@ __device__ __forceinline__ void eff_patch(const Params& P, int k, long long b, f
   constexpr int GPW = 32 / G;  // lane groups per warp
   const bool dc_alone = F.rank == 0 && NG >= kUnits + GPW;
   const int lu0 = !dc_alone ? gid : (gid == NG - GPW ? 0 : (gid < kUnits - 1 ? gid + 1 : kUnits));
+  // the staged spectra must have landed (every thread waits, so none can
+  // leave the kernel with a copy into its shared memory still in flight)
+  if (nst && !mbar_wait_bounded(sbar, 0)) atomicOr(P.err, kErrCopyTimeout);
+  // column of bin u of cached spectrum b (staged: slot si of this CTA) and of bin N/2
+  auto spec_col = [&](const float2* b, int si, int lu, int u) -> const float2* {
+    if (nst) return EFF_IN(si * SC + lu, nst * SC, P.err) ? stage + (si * SC + lu) * SP : stage;
+    return EFF_IN(u, N / 2 + 1, P.err) ? b + (long long)u * N : b;
+  };
+  auto spec_colN = [&](const float2* b, int si) -> const float2* {
+    return nst ? stage + (si * SC + dcN) * SP : b + (long long)(N / 2) * N;
+  };
   for (int lu = lu0; lu < kUnits; lu += dc_alone ? kUnits : NG) {
     const int u = F.rank * kUnits + lu;
     const int col = lu;
     // column spectrum of operand A (u == 0: split into the DC stash)
     float2 a[R];
-    load_column<N, HP>(frame, col, u == 0, dcN, 0, rowsA, g, a);
+    load_column<N, HP>(frame, col, u == 0, dcN, 0, rowsA, g, a, F.rows, F.err);
     fft_fwd<N>(a, g, scr, tw, gmask);
     if (u == 0) dc_split<N>(a, stash, g, gmask);
     if constexpr (OP == OP_SPEC_IMAGE || OP == OP_SPEC_PSF) {
-      store_spectrum<N>(a_out, u, g, a, stash);
+      store_spectrum<N>(a_out, u, g, a, stash, P.err);
     } else if constexpr (OP == OP_FWD_IMAGE || OP == OP_FWD_PSF) {
-      if (a_out) store_spectrum<N>(a_out, u, g, a, stash);
-      column_product<N, false>(a, stash, b0, u, g, scale, a);
+      if (a_out) store_spectrum<N>(a_out, u, g, a, stash, P.err);
+      column_product<N, false>(a, stash, spec_col(b0, 0, lu, u), spec_colN(b0, 0), u, g, scale, a);
       fft_inv<N>(a, g, scr, tw, gmask);
-      store_column<N, HP>(frame, col, u == 0, dcN, 0, P.E0, g, a);
+      store_column<N, HP>(frame, col, u == 0, dcN, 0, P.E0, g, a, F.rows, F.err);
     } else if constexpr (OP == OP_FWD_BOTH) {
       // a holds the image column spectrum (u == 0: packed, split into the DC
       // stash); transform the PSF column through the same code (u == 0: its
       // columns 0 and N/2 packed the same way) and multiply in place.  The DC
       // unit diverges from the other lane groups of its warp only in the
       // splits and the product.
-      if (a_out) store_spectrum<N>(a_out, u, g, a, stash);
+      if (a_out) store_spectrum<N>(a_out, u, g, a, stash, P.err);
       float2 s[R];
-      load_column<N, HP>(frame, col, u == 0, dcN, baseB, P.sf0, g, s);
+      load_column<N, HP>(frame, col, u == 0, dcN, baseB, P.sf0, g, s, F.rows, F.err);
       fft_fwd<N>(s, g, scr, tw, gmask);
       if (u != 0) {
-        if (b_out) store_spectrum<N>(b_out, u, g, s, stash);
+        if (b_out) store_spectrum<N>(b_out, u, g, s, stash, P.err);
 #pragma unroll
         for (int j = 0; j < R; ++j) a[j] = cscale(cmul(a[j], s[j]), scale);
       } else {
         dc_product_split<N>(s, stash, b_out, g, gmask, scale, a);
       }
       fft_inv<N>(a, g, scr, tw, gmask);
-      store_column<N, HP>(frame, col, u == 0, dcN, 0, P.E0, g, a);
+      store_column<N, HP>(frame, col, u == 0, dcN, 0, P.E0, g, a, F.rows, F.err);
     } else {
       // adjoints: output 0 = image (conj F-hat, rows sw0), 1 = PSF (conj X-hat, rows sf0);
       // deconv: the same outputs from the regularised division
@@ -663,13 +814,17 @@ __device__ __forceinline__ void eff_patch(const Params& P, int k, long long b, f
       for (int o = 0; o < 2; ++o) {
         if (o == 0 ? !P.out0 : !P.out1) continue;
         float2 pr[R];
+        const float2* bo = o == 0 ? b0 : b1;
+        const int si = (o == 1 && P.out0) ? 1 : 0;  // staged order: b0 (when used), then b1
+        const float2* c0 = spec_col(bo, si, lu, u);
+        const float2* cN = spec_colN(bo, si);
         if constexpr (OP == OP_DECONV)
-          column_divide<N>(a, stash, o == 0 ? b0 : b1, P.lap, u, g, P.alpha, P.beta, scale, pr);
+          column_divide<N>(a, stash, c0, cN, P.lap, u, g, P.alpha, P.beta, scale, pr);
         else
-          column_product<N, true>(a, stash, o == 0 ? b0 : b1, u, g, scale, pr);
+          column_product<N, true>(a, stash, c0, cN, u, g, scale, pr);
         fft_inv<N>(pr, g, scr, tw, gmask);
         const int base = (o == 1 && P.out0) ? even_up(P.sw0) : 0;
-        store_column<N, HP>(frame, col, u == 0, dcN, base, o == 0 ? P.sw0 : P.sf0, g, pr);
+        store_column<N, HP>(frame, col, u == 0, dcN, base, o == 0 ? P.sw0 : P.sf0, g, pr, F.rows, F.err);
       }
     }
   }
@@ -691,6 +846,20 @@ __device__ __forceinline__ void eff_patch(const Params& P, int k, long long b, f
       c2r_unit<N, CL>(F, 2 * u, v, scr, tw, g, gmask);
       const int ia = i0 + 2 * u;
       const bool rb = 2 * u + 1 < P.E0;
+      if (P.tiles) {
+        // deterministic: the patch's whole E0 x E1 tile, summed by ola_gather
+        float* tl = P.tiles + (b * ((long long)P.csf0 * P.csf1) + T.k) * ((long long)P.E0 * P.E1) +
+                    (long long)(2 * u) * P.E1;
+#pragma unroll
+        for (int mm = 0; mm < R; ++mm) {
+          const int c = g + G * mm;
+          if (c < P.E1) {
+            tl[c] = v[mm].x;
+            if (rb) tl[P.E1 + c] = v[mm].y;
+          }
+        }
+        continue;
+      }
 #pragma unroll
       for (int mm = 0; mm < R; ++mm) {
         const int c = g + G * mm, j = j0 + c;
@@ -736,15 +905,24 @@ __device__ __forceinline__ void eff_patch(const Params& P, int k, long long b, f
         const bool rb = r + 1 < P.sw0;
         const float2 wa = __ldg(P.win0 + T.m * P.sw0 + r);
         const float2 wb = rb ? __ldg(P.win0 + T.m * P.sw0 + r + 1) : make_float2(0.f, 0.f);
+        // deterministic: the patch's whole sw0 x sw1 tile, summed by ola_gather
+        float* tl = P.tiles ? P.tiles + (b * ((long long)P.csf0 * P.csf1) + T.k) * ((long long)P.sw0 * P.sw1) +
+                                  (long long)r * P.sw1
+                            : nullptr;
 #pragma unroll
         for (int mm = 0; mm < R; ++mm) {
           const int c = g + G * mm, j = T.n * P.hop1 + c;
-          if (c < P.sw1 && j < P.sx1) {
+          if (c < P.sw1 && (tl || j < P.sx1)) {
             float w0 = 1.f, w1 = 1.f;
             if constexpr (OP == OP_ADJ) {
               const float2 wc = __ldg(P.win1 + T.n * P.sw1 + c);
               w0 = window_weight(wa, wc);
               w1 = window_weight(wb, wc);
+            }
+            if (tl) {
+              tl[c] = v[mm].x * w0;
+              if (rb) tl[P.sw1 + c] = v[mm].y * w1;
+              continue;
             }
             if (i < P.sx0) atomicAdd(out + (long long)i * P.sx1 + j, v[mm].x * w0);
             if (rb && i + 1 < P.sx0) atomicAdd(out + (long long)(i + 1) * P.sx1 + j, v[mm].y * w1);
@@ -809,7 +987,20 @@ __device__ __forceinline__ void eff_patch(const Params& P, int k, long long b, f
       double d = acc;
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
-      if ((tid & 31) == 0) atomicAdd(P.loss + b, 0.5 * d);
+      if (P.loss_part) {
+        // deterministic: the CTA's share, warps summed in order, stored for
+        // ola_gather (which sums the CTAs' shares in order)
+        __shared__ double warp_part[32];
+        if ((tid & 31) == 0) warp_part[tid >> 5] = d;
+        __syncthreads();
+        if (tid == 0) {
+          double t = 0.0;
+          for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += warp_part[w];
+          P.loss_part[b * ncta + cta] = 0.5 * t;
+        }
+      } else if ((tid & 31) == 0) {
+        atomicAdd(P.loss + b, 0.5 * d);
+      }
     }
   }
   // Peers read this CTA's frame in phase 3: stay resident until they finish.

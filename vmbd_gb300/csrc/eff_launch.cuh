@@ -6,12 +6,16 @@
 namespace eff {
 
 // Shared-memory bytes of one CTA: twiddles + frame (its share of the columns)
-// + per-group exchange scratch + the DC unit's stash (2N).
+// + per-group exchange scratch + the DC unit's stash (2N); with staged
+// spectra (P.stage_spec) also an alignment slot, the staged columns and the
+// mbarrier.
 inline size_t smem_bytes(int N, int op, const Params& P, int threads, int CL) {
   const int R = lane_values(N), G = N / R;
   const int scr = R * (G + 1) + 8;
-  return sizeof(float2) * ((size_t)N + (size_t)frame_rows(P, op) * frame_pitch(N, CL) +
-                           (size_t)(threads / G) * scr + 2 * (size_t)N);
+  size_t n = (size_t)N + (size_t)frame_rows(P, op) * frame_pitch(N, CL) + (size_t)(threads / G) * scr +
+             2 * (size_t)N;
+  if (const int nst = staged_specs(P, op)) n += 1 + (size_t)nst * staged_cols(N, CL) * (N + kSpecPad) + 1;
+  return sizeof(float2) * n;
 }
 
 template <int N, int OP, int CL>

@@ -30,10 +30,13 @@ class EffPlan:
     """Plan for ``y = EFF(x, f)`` on one geometry (OlaGPU.__init__,
     olaGPU.py:95-168, without the cached spectrum)."""
 
-    def __init__(self, winaux: Winaux, sf, mode: str = "valid", sfft: int = 0, device=None, threads: int = 0):
+    def __init__(self, winaux: Winaux, sf, mode: str = "valid", sfft: int = 0, device=None, threads: int = 0,
+                 deterministic: bool = False, lib=None):
         if mode not in _lib.MODES:
             raise NotImplementedError("Not a valid mode!")
-        self.lib = _lib.load()
+        # lib: the library to run on (default the product library; tests pass
+        # the bounds-checked variant, _lib.load_debug())
+        self.lib = lib if lib is not None else _lib.load()
         self.winaux = winaux
         self.sf = (int(sf[0]), int(sf[1]))
         self.sx = winaux.sx
@@ -50,6 +53,10 @@ class EffPlan:
         g.sfft = int(sfft)
         g.threads = int(threads)
         g.mode = _lib.MODES[mode]
+        # deterministic: overlap-add by a fixed-order gather (bit-identical
+        # repeats; one extra kernel per overlap-added output)
+        g.flags = _lib.GEOM_DETERMINISTIC if deterministic else 0
+        self.deterministic = bool(deterministic)
         self._w0 = np.ascontiguousarray(winaux.win0, dtype=np.float32)
         self._w1 = np.ascontiguousarray(winaux.win1, dtype=np.float32)
         h = ctypes.c_void_p()
@@ -78,6 +85,14 @@ class EffPlan:
             except Exception:
                 pass
             self._h = None
+
+    def device_errors(self, clear: bool = True) -> int:
+        """Error bits the plan's kernels recorded on the device (waits for
+        the device; ``EFF_DEVERR_*`` of include/vmbd_eff.h)."""
+        v = ctypes.c_int()
+        with torch.cuda.device(self.device):
+            _lib.check(self.lib.eff_plan_device_errors(self._h, ctypes.byref(v), int(clear)))
+        return v.value
 
     # ------------------------------------------------------------------
     @property
