@@ -41,7 +41,7 @@ def load(path):
     d = {k: z[k] for k in z.files}
     d["mode"] = str(d["mode"])
     d["name"] = os.path.basename(path)[4:-4]
-    if "r" not in d:
+    if "r_sum" in d:
         r = np.random.default_rng(int(d["seed"]) + 200).standard_normal(d["y"].shape).astype(np.float32)
         if not np.allclose(_sums(r), d["r_sum"], rtol=1e-12, atol=0):
             raise AssertionError(f"{d['name']}: regenerated residual differs from the fixture's")

@@ -141,7 +141,9 @@ def _bind(L: ctypes.CDLL) -> ctypes.CDLL:
     return L
 
 
-def check(status: int) -> None:
+def check(status: int, lib=None) -> None:
+    """Raise EffError for a non-OK status with the message of the library the
+    call went to (default the product library)."""
     if status != EFF_OK:
-        msg = load().eff_last_error().decode(errors="replace")
+        msg = (lib or load()).eff_last_error().decode(errors="replace")
         raise EffError(status, msg)

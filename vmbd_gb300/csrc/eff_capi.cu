@@ -121,7 +121,11 @@ int launch_kernel(const EffPlan* p, int op, const eff::Params& P, int batch, int
     case 512: e = eff::launch_n512(op, CL, P, p->K, batch, threads, smem, st); break;
     default: return fail(EFF_ERR_UNSUPPORTED, "frame size");
   }
-  if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
+  if (e != cudaSuccess)
+    return cuda_fail(e, ("kernel launch (frame " + std::to_string(p->N) + ", op " + std::to_string(op) + ", " +
+                         std::to_string(CL) + " CTA(s) per patch, " + std::to_string(threads) + " threads, " +
+                         std::to_string(smem) + " B shared)")
+                            .c_str());
   return EFF_OK;
 }
 

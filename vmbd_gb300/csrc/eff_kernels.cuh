@@ -220,6 +220,17 @@ struct Frame {
   static constexpr int kDcN = W;  // local column of bin N/2 (CTA 0; the DC unit packs it with column 0)
 };
 
+// One overlap-add contribution: an atomic add into the output image, or, for
+// a deterministic plan, a plain store into the patch's tile (every tile
+// element is written once).  One predicated pair of instructions, so that the
+// epilogues keep a single code path for both.
+__device__ __forceinline__ void ola_put(float* p, float v, bool tile) {
+  asm volatile(
+      "{\n .reg .pred q;\n setp.ne.u32 q, %2, 0;\n @q st.global.f32 [%0], %1;\n @!q red.global.add.f32 [%0], %1;\n}" ::"l"(p),
+      "f"(v), "r"((unsigned)tile)
+      : "memory");
+}
+
 // Window weight ws[k=(m,n)][r][c] from the per-dim (alpha, gamma) tables:
 // alpha*alpha' inside the image, gamma*gamma' = 1/(patches covering the
 // pixel) on the outermost rows/columns that only zero-valued window samples
@@ -726,27 +737,31 @@ __device__ __forceinline__ void eff_patch(const Params& P, int k, long long b, f
   {
     const int nA = (rowsA + 1) >> 1;
     const int nB = has_b(OP) ? (P.sf0 + 1) >> 1 : 0;
-    auto transform_unit = [&](int u, float2 (&v)[R], float2 (&p)[R]) -> int {
-      int row;
-      if (u < nA) {
-        load_rows<N, A>(P, T, 2 * u, g, v);
-        row = 2 * u;
-      } else {
-        load_rows<N, OPND_PSF>(P, T, 2 * (u - nA), g, v);
-        row = baseB + 2 * (u - nA);
+    // (one loop, so that the transform code exists once: every thread takes
+    // the first iteration and meets the barrier there)
+    bool first = true;
+#pragma unroll 1
+    for (int u = wid;; u += NW) {
+      float2 v[R], p[R];
+      int row = -1;
+      if (u < nA + nB) {
+        if (u < nA) {
+          load_rows<N, A>(P, T, 2 * u, g, v);
+          row = 2 * u;
+        } else {
+          load_rows<N, OPND_PSF>(P, T, 2 * (u - nA), g, v);
+          row = baseB + 2 * (u - nA);
+        }
+        r2c_transform<N>(v, p, scr, tw, g, gmask);
       }
-      r2c_transform<N>(v, p, scr, tw, g, gmask);
-      return row;
-    };
-    float2 v[R], p[R];
-    int row = -1;
-    if (wid < nA + nB) row = transform_unit(wid, v, p);
-    // The peer must not write into this CTA's frame before it is running (and,
-    // in a persistent loop, before this CTA has finished the previous patch).
-    phase_sync();
-    if (row >= 0) r2c_scatter<N, CL>(v, p, F, row, g);
-    for (int u = wid + NW; u < nA + nB; u += NW) {
-      row = transform_unit(u, v, p);
+      if (first) {
+        // The peer must not write into this CTA's frame before it is running
+        // (and, in a persistent loop, before this CTA has finished the
+        // previous patch).
+        phase_sync();
+        first = false;
+      }
+      if (row < 0) break;
       r2c_scatter<N, CL>(v, p, F, row, g);
     }
   }
@@ -846,26 +861,22 @@ __device__ __forceinline__ void eff_patch(const Params& P, int k, long long b, f
       c2r_unit<N, CL>(F, 2 * u, v, scr, tw, g, gmask);
       const int ia = i0 + 2 * u;
       const bool rb = 2 * u + 1 < P.E0;
-      if (P.tiles) {
-        // deterministic: the patch's whole E0 x E1 tile, summed by ola_gather
-        float* tl = P.tiles + (b * ((long long)P.csf0 * P.csf1) + T.k) * ((long long)P.E0 * P.E1) +
-                    (long long)(2 * u) * P.E1;
-#pragma unroll
-        for (int mm = 0; mm < R; ++mm) {
-          const int c = g + G * mm;
-          if (c < P.E1) {
-            tl[c] = v[mm].x;
-            if (rb) tl[P.E1 + c] = v[mm].y;
-          }
-        }
-        continue;
-      }
+      // deterministic: the patch's whole E0 x E1 tile, summed by ola_gather
+      // (tile row 2u at column c); else the image at row ia, column j0 + c
+      const bool tile = P.tiles != nullptr;
+      float* dst = tile ? P.tiles + (b * ((long long)P.csf0 * P.csf1) + T.k) * ((long long)P.E0 * P.E1) +
+                              (long long)(2 * u) * P.E1
+                        : out + (long long)ia * P.sy1 + j0;
+      const long long pitch = tile ? P.E1 : P.sy1;
+      const bool okA = tile || (ia >= 0 && ia < P.sy0);
+      const bool okB = rb && (tile || (ia + 1 >= 0 && ia + 1 < P.sy0));
+      const int clo = tile ? 0 : max(0, -j0), chi = tile ? P.E1 : min(P.E1, P.sy1 - j0);
 #pragma unroll
       for (int mm = 0; mm < R; ++mm) {
-        const int c = g + G * mm, j = j0 + c;
-        if (c < P.E1 && j >= 0 && j < P.sy1) {
-          if (ia >= 0 && ia < P.sy0) atomicAdd(out + (long long)ia * P.sy1 + j, v[mm].x);
-          if (rb && ia + 1 >= 0 && ia + 1 < P.sy0) atomicAdd(out + (long long)(ia + 1) * P.sy1 + j, v[mm].y);
+        const int c = g + G * mm;
+        if (c >= clo && c < chi) {
+          if (okA) ola_put(dst + c, v[mm].x, tile);
+          if (okB) ola_put(dst + pitch + c, v[mm].y, tile);
         }
       }
     }
@@ -905,27 +916,28 @@ __device__ __forceinline__ void eff_patch(const Params& P, int k, long long b, f
         const bool rb = r + 1 < P.sw0;
         const float2 wa = __ldg(P.win0 + T.m * P.sw0 + r);
         const float2 wb = rb ? __ldg(P.win0 + T.m * P.sw0 + r + 1) : make_float2(0.f, 0.f);
-        // deterministic: the patch's whole sw0 x sw1 tile, summed by ola_gather
-        float* tl = P.tiles ? P.tiles + (b * ((long long)P.csf0 * P.csf1) + T.k) * ((long long)P.sw0 * P.sw1) +
-                                  (long long)r * P.sw1
-                            : nullptr;
+        // deterministic: the patch's whole sw0 x sw1 tile (row r, column c),
+        // summed by ola_gather; else the image at row i, column n hop1 + c
+        const bool tile = P.tiles != nullptr;
+        float* dst = tile ? P.tiles + (b * ((long long)P.csf0 * P.csf1) + T.k) * ((long long)P.sw0 * P.sw1) +
+                                (long long)r * P.sw1
+                          : out + (long long)i * P.sx1 + T.n * P.hop1;
+        const long long pitch = tile ? P.sw1 : P.sx1;
+        const bool okA = tile || i < P.sx0;
+        const bool okB = rb && (tile || i + 1 < P.sx0);
+        const int chi = tile ? P.sw1 : min(P.sw1, P.sx1 - T.n * P.hop1);
 #pragma unroll
         for (int mm = 0; mm < R; ++mm) {
-          const int c = g + G * mm, j = T.n * P.hop1 + c;
-          if (c < P.sw1 && (tl || j < P.sx1)) {
+          const int c = g + G * mm;
+          if (c < chi) {
             float w0 = 1.f, w1 = 1.f;
             if constexpr (OP == OP_ADJ) {
               const float2 wc = __ldg(P.win1 + T.n * P.sw1 + c);
               w0 = window_weight(wa, wc);
               w1 = window_weight(wb, wc);
             }
-            if (tl) {
-              tl[c] = v[mm].x * w0;
-              if (rb) tl[P.sw1 + c] = v[mm].y * w1;
-              continue;
-            }
-            if (i < P.sx0) atomicAdd(out + (long long)i * P.sx1 + j, v[mm].x * w0);
-            if (rb && i + 1 < P.sx0) atomicAdd(out + (long long)(i + 1) * P.sx1 + j, v[mm].y * w1);
+            if (okA) ola_put(dst + c, v[mm].x * w0, tile);
+            if (okB) ola_put(dst + pitch + c, v[mm].y * w1, tile);
           }
         }
       } else {

@@ -25,6 +25,9 @@ cudaError_t launch_one(const Params& P, int K, int batch, int threads, size_t sm
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   auto kern = eff_kernel<N, OP, CL>;
+  // an error status an earlier runtime call left behind (already returned to
+  // its caller) must not be read back as this launch's result below
+  (void)cudaGetLastError();
   if (dev >= 64 || attr_bytes[dev].load() < (int)smem) {
     e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;

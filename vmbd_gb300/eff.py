@@ -61,11 +61,11 @@ class EffPlan:
         self._w1 = np.ascontiguousarray(winaux.win1, dtype=np.float32)
         h = ctypes.c_void_p()
         with torch.cuda.device(self.device):
-            _lib.check(self.lib.eff_plan_create(ctypes.byref(g), self._w0.ctypes.data,
+            self._st(self.lib.eff_plan_create(ctypes.byref(g), self._w0.ctypes.data,
                                                 self._w1.ctypes.data, ctypes.byref(h)))
         self._h = h
         n = ctypes.c_int()
-        _lib.check(self.lib.eff_plan_frame(h, ctypes.byref(n)))
+        self._st(self.lib.eff_plan_frame(h, ctypes.byref(n)))
         self.N = n.value
         self.K = winaux.K
         off = {"valid": [v - 1 for v in self.sf], "same": [v // 2 for v in self.sf], "full": [0, 0]}
@@ -86,12 +86,15 @@ class EffPlan:
                 pass
             self._h = None
 
+    def _st(self, status: int) -> None:
+        _lib.check(status, self.lib)
+
     def device_errors(self, clear: bool = True) -> int:
         """Error bits the plan's kernels recorded on the device (waits for
         the device; ``EFF_DEVERR_*`` of include/vmbd_eff.h)."""
         v = ctypes.c_int()
         with torch.cuda.device(self.device):
-            _lib.check(self.lib.eff_plan_device_errors(self._h, ctypes.byref(v), int(clear)))
+            self._st(self.lib.eff_plan_device_errors(self._h, ctypes.byref(v), int(clear)))
         return v.value
 
     # ------------------------------------------------------------------
@@ -128,13 +131,13 @@ class EffPlan:
     def psf_spectrum(self, f, out=None):
         f, b = self._check(f, (self.K,) + self.sf, "f")
         out = self.empty_spectrum(b) if out is None else self._check_spec(out, b, "out")
-        _lib.check(self.lib.eff_psf_spectrum(self._h, _ptr(f), _ptr(out), b or 1, _stream(self.device)))
+        self._st(self.lib.eff_psf_spectrum(self._h, _ptr(f), _ptr(out), b or 1, _stream(self.device)))
         return out
 
     def image_spectrum(self, x, out=None):
         x, b = self._check(x, self.sx, "x")
         out = self.empty_spectrum(b) if out is None else self._check_spec(out, b, "out")
-        _lib.check(self.lib.eff_image_spectrum(self._h, _ptr(x), _ptr(out), b or 1, _stream(self.device)))
+        self._st(self.lib.eff_image_spectrum(self._h, _ptr(x), _ptr(out), b or 1, _stream(self.device)))
         return out
 
     def forward_image(self, x, fhat, out=None, xhat_out=None):
@@ -145,7 +148,7 @@ class EffPlan:
             self._check_spec(xhat_out, b, "xhat_out")
         if out is None:
             out = torch.empty(((b,) if b else ()) + self.sy, dtype=torch.float32, device=self.device)
-        _lib.check(self.lib.eff_forward_image(self._h, _ptr(x), _ptr(fhat), _ptr(out), _ptr(xhat_out),
+        self._st(self.lib.eff_forward_image(self._h, _ptr(x), _ptr(fhat), _ptr(out), _ptr(xhat_out),
                                               b or 1, _stream(self.device)))
         return out
 
@@ -157,7 +160,7 @@ class EffPlan:
             self._check_spec(fhat_out, b, "fhat_out")
         if out is None:
             out = torch.empty(((b,) if b else ()) + self.sy, dtype=torch.float32, device=self.device)
-        _lib.check(self.lib.eff_forward_psf(self._h, _ptr(f), _ptr(xhat), _ptr(out), _ptr(fhat_out),
+        self._st(self.lib.eff_forward_psf(self._h, _ptr(f), _ptr(xhat), _ptr(out), _ptr(fhat_out),
                                             b or 1, _stream(self.device)))
         return out
 
@@ -179,11 +182,11 @@ class EffPlan:
             subtract, bs = self._check(subtract, self.sy, "subtract")
             if bs != b:
                 raise IOError("Size missmatch: x and subtract batch dims differ")
-            _lib.check(self.lib.eff_forward_residual(self._h, _ptr(x), _ptr(f), _ptr(subtract), _ptr(out),
+            self._st(self.lib.eff_forward_residual(self._h, _ptr(x), _ptr(f), _ptr(subtract), _ptr(out),
                                                      _ptr(xhat_out), _ptr(fhat_out), b or 1,
                                                      _stream(self.device)))
             return out
-        _lib.check(self.lib.eff_forward_both(self._h, _ptr(x), _ptr(f), _ptr(out), _ptr(xhat_out),
+        self._st(self.lib.eff_forward_both(self._h, _ptr(x), _ptr(f), _ptr(out), _ptr(xhat_out),
                                              _ptr(fhat_out), b or 1, _stream(self.device)))
         return out
 
@@ -214,7 +217,7 @@ class EffPlan:
         gx = gx if want_image else None
         gf = gf if want_psf else None
         ws = self.workspace(b)
-        _lib.check(self.lib.eff_loss_grad(self._h, _ptr(x), _ptr(f), _ptr(y_obs), _ptr(loss), _ptr(gx),
+        self._st(self.lib.eff_loss_grad(self._h, _ptr(x), _ptr(f), _ptr(y_obs), _ptr(loss), _ptr(gx),
                                           _ptr(gf), _ptr(ws), ws.numel(), b or 1, _stream(self.device)))
         return loss, gx, gf
 
@@ -265,12 +268,12 @@ class EffPlan:
                 loss = None
             elif loss is None:
                 loss = torch.empty(lead, dtype=torch.float64, device=self.device)
-            _lib.check(self.lib.eff_adjoint_ex(self._h, _ptr(y), None, None, _ptr(fhat if want_image else None),
+            self._st(self.lib.eff_adjoint_ex(self._h, _ptr(y), None, None, _ptr(fhat if want_image else None),
                                                _ptr(xhat if want_psf else None), _ptr(gx), _ptr(gf), _ptr(loss),
                                                mode, _lib.LOSS_OF_Y, b or 1, _stream(self.device)))
             return loss, gx, gf
         if y_obs is None:
-            _lib.check(self.lib.eff_adjoint(self._h, _ptr(y), _ptr(fhat if want_image else None),
+            self._st(self.lib.eff_adjoint(self._h, _ptr(y), _ptr(fhat if want_image else None),
                                             _ptr(xhat if want_psf else None), _ptr(gx), _ptr(gf), mode,
                                             b or 1, _stream(self.device)))
             return gx, gf
@@ -279,7 +282,7 @@ class EffPlan:
             loss = None
         elif loss is None:
             loss = torch.empty(lead, dtype=torch.float64, device=self.device)
-        _lib.check(self.lib.eff_adjoint_residual(self._h, _ptr(y), _ptr(y_obs),
+        self._st(self.lib.eff_adjoint_residual(self._h, _ptr(y), _ptr(y_obs),
                                                  _ptr(fhat if want_image else None),
                                                  _ptr(xhat if want_psf else None), _ptr(gx), _ptr(gf),
                                                  _ptr(loss), mode, b or 1, _stream(self.device)))
@@ -305,7 +308,7 @@ class EffPlan:
             self._check_spec(xhat, b, "xhat")
             if fz is None:
                 fz = torch.empty(lead + (self.K,) + self.sf, dtype=torch.float32, device=self.device)
-        _lib.check(self.lib.eff_deconv_xdirect(self._h, _ptr(y), _ptr(fhat), _ptr(xhat),
+        self._st(self.lib.eff_deconv_xdirect(self._h, _ptr(y), _ptr(fhat), _ptr(xhat),
                                                _ptr(u if fhat is not None else None),
                                                _ptr(fz if xhat is not None else None), float(alpha),
                                                float(beta), b or 1, _stream(self.device)))
@@ -347,6 +350,9 @@ class EffBatch:
     (``eff_batch_*``).  Per class c, arrays carry a leading dim of
     ``counts[c]`` images."""
 
+    def _st(self, status: int) -> None:
+        _lib.check(status, self.lib)
+
     def __init__(self, plans, counts):
         if len(plans) != len(counts) or not plans:
             raise ValueError("one count per plan")
@@ -359,7 +365,7 @@ class EffBatch:
         cnt = (ctypes.c_int * n)(*self.counts)
         h = ctypes.c_void_p()
         with torch.cuda.device(self.device):
-            _lib.check(self.lib.eff_batch_create(arr, cnt, n, ctypes.byref(h)))
+            self._st(self.lib.eff_batch_create(arr, cnt, n, ctypes.byref(h)))
         self._h = h
         self._work = None
 
@@ -397,11 +403,11 @@ class EffBatch:
             ys = [torch.empty((c,) + p.sy, device=self.device) for p, c in zip(self.plans, self.counts)]
         if subtracts is not None:
             self._shapes(subtracts, lambda p: p.sy, "subtract")
-            _lib.check(self.lib.eff_batch_forward_residual(
+            self._st(self.lib.eff_batch_forward_residual(
                 self._h, self._ptrs(xs), self._ptrs(fs), self._ptrs(subtracts), self._ptrs(ys),
                 self._ptrs(xhats), self._ptrs(fhats), _stream(self.device)))
             return ys
-        _lib.check(self.lib.eff_batch_forward_both(self._h, self._ptrs(xs), self._ptrs(fs), self._ptrs(ys),
+        self._st(self.lib.eff_batch_forward_both(self._h, self._ptrs(xs), self._ptrs(fs), self._ptrs(ys),
                                                    self._ptrs(xhats), self._ptrs(fhats), _stream(self.device)))
         return ys
 
@@ -414,7 +420,7 @@ class EffBatch:
             gfs = [torch.empty((c, p.K) + p.sf, device=self.device) for p, c in zip(self.plans, self.counts)]
         if losses is None:
             losses = [torch.empty(c, dtype=torch.float64, device=self.device) for c in self.counts]
-        _lib.check(self.lib.eff_batch_adjoint_residual(
+        self._st(self.lib.eff_batch_adjoint_residual(
             self._h, self._ptrs(ys), self._ptrs(y_obss), self._ptrs(fhats), self._ptrs(xhats),
             self._ptrs(gxs), self._ptrs(gfs), self._ptrs(losses), _stream(self.device)))
         return losses, gxs, gfs
