@@ -35,6 +35,14 @@
 
 #include <stddef.h>
 
+/* The library is built with hidden symbol visibility; only these entry
+ * points are exported. */
+#if defined(__GNUC__)
+#define EFF_API __attribute__((visibility("default")))
+#else
+#define EFF_API
+#endif
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -87,51 +95,51 @@ typedef struct EffPlan EffPlan;
 /* Replaces OlaGPU.__init__'s geometry checks (olaGPU.py:95-168) and the
  * window upload of win2winaux (imagetools.py:437-454).  win0 [csf0*sw0*2] and
  * win1 [csf1*sw1*2] are HOST arrays; the plan keeps device copies. */
-int eff_plan_create(const EffGeom* geom, const float* win0, const float* win1, EffPlan** plan);
-int eff_plan_destroy(EffPlan* plan);
+EFF_API int eff_plan_create(const EffGeom* geom, const float* win0, const float* win1, EffPlan** plan);
+EFF_API int eff_plan_destroy(EffPlan* plan);
 
 /* FFT frame edge chosen by the plan, and the bytes of one image's cached
  * spectrum (K * (N/2+1) * N complex64). */
-int eff_plan_frame(const EffPlan* plan, int* n);
-size_t eff_spectrum_bytes(const EffPlan* plan);
+EFF_API int eff_plan_frame(const EffPlan* plan, int* n);
+EFF_API size_t eff_spectrum_bytes(const EffPlan* plan);
 
 /* PSF spectrum cache of an F object: pad_stack_GPU + FFT, olaGPU.py:142-157.
  * f [batch, K, sf0, sf1] -> fhat [batch, spectrum]. */
-int eff_psf_spectrum(const EffPlan* plan, const float* f, void* fhat, int batch, void* stream);
+EFF_API int eff_psf_spectrum(const EffPlan* plan, const float* f, void* fhat, int batch, void* stream);
 
 /* Windowed-patch spectrum cache of an X object: chop_mod_pad_GPU + FFT,
  * olaGPU.py:147-157.  x [batch, sx0, sx1] -> xhat. */
-int eff_image_spectrum(const EffPlan* plan, const float* x, void* xhat, int batch, void* stream);
+EFF_API int eff_image_spectrum(const EffPlan* plan, const float* x, void* xhat, int batch, void* stream);
 
 /* F.cnv(x), olaGPU.py:170-257: y = crop(OLA(IFFT(fhat * FFT(ws * chop(x))))).
  * y [batch, sy0, sy1] is overwritten.  xhat_out (nullable) receives the
  * windowed-patch spectrum of x as eff_image_spectrum would. */
-int eff_forward_image(const EffPlan* plan, const float* x, const void* fhat, float* y,
+EFF_API int eff_forward_image(const EffPlan* plan, const float* x, const void* fhat, float* y,
                       void* xhat_out, int batch, void* stream);
 
 /* X.cnv(f), olaGPU.py:170-257 with the X object: same operator, the PSFs
  * transformed in-kernel.  fhat_out (nullable) receives f's spectrum. */
-int eff_forward_psf(const EffPlan* plan, const float* f, const void* xhat, float* y,
+EFF_API int eff_forward_psf(const EffPlan* plan, const float* f, const void* xhat, float* y,
                     void* fhat_out, int batch, void* stream);
 
 /* F.cnvtp(y) and X.cnvtp(y), olaGPU.py:261-311, sharing one transform of y.
  * gx [batch, sx0, sx1] (needs fhat) and/or gf [batch, K, sf0, sf1] (needs
  * xhat) are overwritten; pass NULL for an output that is not wanted.
  * adj_mode: EFF_ADJ_EXACT or EFF_ADJ_REFERENCE. */
-int eff_adjoint(const EffPlan* plan, const float* y, const void* fhat, const void* xhat, float* gx,
+EFF_API int eff_adjoint(const EffPlan* plan, const float* y, const void* fhat, const void* xhat, float* gx,
                 float* gf, int adj_mode, int batch, void* stream);
 
 /* y = EFF(x, f) from the raw image and PSFs in one kernel (the forward of an
  * autograd step): both operands are transformed in-kernel.  xhat_out /
  * fhat_out (nullable) receive the two spectra for a later eff_adjoint. */
-int eff_forward_both(const EffPlan* plan, const float* x, const float* f, float* y, void* xhat_out,
+EFF_API int eff_forward_both(const EffPlan* plan, const float* x, const float* f, float* y, void* xhat_out,
                      void* fhat_out, int batch, void* stream);
 
 /* eff_adjoint of the residual r = y - y_obs (both [batch, sy0, sy1]) without
  * forming r; loss (nullable, double [batch]) receives 0.5 * ||y - y_obs||^2.
  * The gradient of that loss w.r.t. x and f (cnvinv_objfun/gradfun without
  * regularisation, olaGPU.py:756-811). */
-int eff_adjoint_residual(const EffPlan* plan, const float* y, const float* y_obs, const void* fhat,
+EFF_API int eff_adjoint_residual(const EffPlan* plan, const float* y, const float* y_obs, const void* fhat,
                          const void* xhat, float* gx, float* gf, double* loss, int adj_mode,
                          int batch, void* stream);
 
@@ -140,7 +148,7 @@ int eff_adjoint_residual(const EffPlan* plan, const float* y, const float* y_obs
  * (the additions commute with the overlap-add).  An adjoint of r with
  * EFF_LOSS_OF_Y then reads one plane instead of y and y_obs; eff_loss_grad
  * is these two kernels.  r must not alias y_obs. */
-int eff_forward_residual(const EffPlan* plan, const float* x, const float* f, const float* y_obs, float* r,
+EFF_API int eff_forward_residual(const EffPlan* plan, const float* x, const float* f, const float* y_obs, float* r,
                          void* xhat_out, void* fhat_out, int batch, void* stream);
 
 /* One loss/gradient step of 0.5 * ||EFF(x, f) - y_obs||^2: eff_forward_residual
@@ -148,8 +156,8 @@ int eff_forward_residual(const EffPlan* plan, const float* x, const float* f, co
  * the two spectra in a caller-provided device workspace of at least
  * eff_loss_grad_workspace_bytes(plan, batch) bytes.  gx or gf may be NULL
  * (not both); loss may be NULL. */
-size_t eff_loss_grad_workspace_bytes(const EffPlan* plan, int batch);
-int eff_loss_grad(const EffPlan* plan, const float* x, const float* f, const float* y_obs,
+EFF_API size_t eff_loss_grad_workspace_bytes(const EffPlan* plan, int batch);
+EFF_API int eff_loss_grad(const EffPlan* plan, const float* x, const float* f, const float* y_obs,
                   double* loss, float* gx, float* gf, void* workspace, size_t workspace_bytes,
                   int batch, void* stream);
 
@@ -167,8 +175,8 @@ int eff_loss_grad(const EffPlan* plan, const float* x, const float* f, const flo
  * it again on a device after cudaDeviceReset of that device (the address may
  * change).  All calls share the array; calls whose GPU work overlaps (other
  * streams or threads) race on it.  Allocates nothing. */
-size_t eff_static_scratch_bytes(void);
-int eff_loss_grad_static(const EffPlan* plan, const float* x, const float* f, const float* y_obs,
+EFF_API size_t eff_static_scratch_bytes(void);
+EFF_API int eff_loss_grad_static(const EffPlan* plan, const float* x, const float* f, const float* y_obs,
                          double* loss, float* gx, float* gf, int batch, void* stream);
 
 /* PSF projections on [K, n] stacks (n = sf0*sf1), in place.
@@ -177,18 +185,18 @@ int eff_loss_grad_static(const EffPlan* plan, const float* x, const float* f, co
  * EFF_PROJ_SIMPLEX: Euclidean projection onto {f >= 0, sum f = 1}. */
 #define EFF_PROJ_CLIP_NORMALIZE 0
 #define EFF_PROJ_SIMPLEX 1
-int eff_project_psf(float* f, int K, int n, int proj_mode, void* stream);
+EFF_API int eff_project_psf(float* f, int K, int n, int proj_mode, void* stream);
 
 /* projection.cu:3-27 as intended: w[b] = <fs, basis[b]> for b < nb, with
  * fs [n] and basis [nb, n]. */
-int eff_basis_project(const float* fs, const float* basis, float* w, int nb, int n, void* stream);
+EFF_API int eff_basis_project(const float* fs, const float* basis, float* w, int nb, int n, void* stream);
 
 /* edgetaper_gpu (gputools.py:643-673, edgetaper.cu:6-31), in place on
  * [batch, rows, cols]: row i < hy is scaled by wy[i], row i > rows-1-hy by
  * wy[rows-1-i]; columns likewise with wx.  wy [hy], wx [hx] are DEVICE
  * tables (the first floor(sf/2) samples of the Bartlett-Hann window over
  * the product of the two windows' maxima, sf made odd). */
-int eff_edgetaper(float* im, int rows, int cols, const float* wy, int hy, const float* wx, int hx,
+EFF_API int eff_edgetaper(float* im, int rows, int cols, const float* wy, int hy, const float* wx, int hx,
                   int batch, void* stream);
 
 /* Fourier-division deconvolution, OlaGPU.deconv(y, mode='xdirect'),
@@ -205,12 +213,12 @@ int eff_edgetaper(float* im, int rows, int cols, const float* wy, int hy, const 
  * happens in the plan's frame, so results equal the reference's when the
  * plan's N is the reference's frame (the power of two >= sw + sf - 1 in
  * both dims).  EFF_ERR_UNSUPPORTED for mode full (olaGPU.py:570-571). */
-int eff_deconv_xdirect(const EffPlan* plan, const float* y, const void* fhat, const void* xhat, float* u,
+EFF_API int eff_deconv_xdirect(const EffPlan* plan, const float* y, const void* fhat, const void* xhat, float* u,
                        float* fz, float alpha, float beta, int batch, void* stream);
 
 /* eff_adjoint of mask .* y (mask [batch, sy0, sy1]) without forming the
  * product: Ft(m y) of the multiplicative image step, vmbd_chimney.py:143. */
-int eff_adjoint_masked(const EffPlan* plan, const float* y, const float* mask, const void* fhat,
+EFF_API int eff_adjoint_masked(const EffPlan* plan, const float* y, const float* mask, const void* fhat,
                        const void* xhat, float* gx, float* gf, int adj_mode, int batch, void* stream);
 
 /* Chained calls without memsets.  Loops that run many forward / adjoint
@@ -229,10 +237,10 @@ int eff_adjoint_masked(const EffPlan* plan, const float* y, const float* mask, c
  *   eff_adjoint_masked (mask) in one; flags EFF_OUT_ZEROED: gx and loss are
  *   already zero; EFF_LOSS_OF_Y (no y_obs, no mask): y is the residual, as
  *   eff_forward_residual leaves it, and loss (nullable) += 0.5 * sum y^2. */
-int eff_forward_ex(const EffPlan* plan, int operand, const float* u, const void* spec, float* y, const float* sub,
+EFF_API int eff_forward_ex(const EffPlan* plan, int operand, const float* u, const void* spec, float* y, const float* sub,
                    void* spec_out, int flags, float* zero_f, long long zero_nf, double* zero_d, int zero_nd,
                    int batch, void* stream);
-int eff_adjoint_ex(const EffPlan* plan, const float* y, const float* y_obs, const float* mask, const void* fhat,
+EFF_API int eff_adjoint_ex(const EffPlan* plan, const float* y, const float* y_obs, const float* mask, const void* fhat,
                    const void* xhat, float* gx, float* gf, double* loss, int adj_mode, int flags, int batch,
                    void* stream);
 /* eff_forward_both (sub NULL) / eff_forward_residual (sub = y_obs, not
@@ -240,7 +248,7 @@ int eff_adjoint_ex(const EffPlan* plan, const float* y, const float* y_obs, cons
  * eff_loss_grad is: memset of its residual buffer, this call with
  * EFF_OUT_ZEROED clearing gx and loss, eff_adjoint_ex with
  * EFF_OUT_ZEROED | EFF_LOSS_OF_Y. */
-int eff_forward_both_ex(const EffPlan* plan, const float* x, const float* f, const float* sub, float* y,
+EFF_API int eff_forward_both_ex(const EffPlan* plan, const float* x, const float* f, const float* sub, float* y,
                         void* xhat_out, void* fhat_out, int flags, float* zero_f, long long zero_nf, double* zero_d,
                         int zero_nd, int batch, void* stream);
 
@@ -266,12 +274,12 @@ int eff_forward_both_ex(const EffPlan* plan, const float* x, const float* f, con
  * flags EFF_OUT_ZEROED: out (eff_dots3) / xmax_bits (eff_mu_update) is
  * already zero; zero_f[0, zero_n) (nullable) is cleared as a side job, as in
  * eff_forward_ex. */
-int eff_dots3(const float* a, const float* ap, long long na, const float* b, const float* bp, long long nb,
+EFF_API int eff_dots3(const float* a, const float* ap, long long na, const float* b, const float* bp, long long nb,
               double* out, int flags, void* stream);
-int eff_pg_step(float* f, const float* g, float* f_prev, float* g_prev, int K, int n, const double* dots,
+EFF_API int eff_pg_step(float* f, const float* g, float* f_prev, float* g_prev, int K, int n, const double* dots,
                 int mode, float* state, float* zero_f, long long zero_n, void* stream);
-int eff_max_nonneg(const float* a, long long n, unsigned* out_bits, void* stream);
-int eff_mu_update(float* x, const float* num, const float* den, float tol, int rows, int cols, int border0,
+EFF_API int eff_max_nonneg(const float* a, long long n, unsigned* out_bits, void* stream);
+EFF_API int eff_mu_update(float* x, const float* num, const float* den, float tol, int rows, int cols, int border0,
                   int border1, const unsigned* num_max_bits, float floor_rel, unsigned* xmax_bits, int flags,
                   float* zero_f, long long zero_n, void* stream);
 
@@ -285,20 +293,20 @@ int eff_mu_update(float* x, const float* num, const float* den, float tol, int r
  * device pointers (host arrays); outputs accumulated with atomics (y, gx,
  * loss) are cleared by the call. */
 typedef struct EffBatch EffBatch;
-int eff_batch_create(const EffPlan* const* plans, const int* counts, int n_classes, EffBatch** batch);
-int eff_batch_destroy(EffBatch* batch);
-int eff_batch_items(const EffBatch* batch);
+EFF_API int eff_batch_create(const EffPlan* const* plans, const int* counts, int n_classes, EffBatch** batch);
+EFF_API int eff_batch_destroy(EffBatch* batch);
+EFF_API int eff_batch_items(const EffBatch* batch);
 /* eff_forward_both over the batch: x, f -> y (+ both spectra, nullable). */
-int eff_batch_forward_both(const EffBatch* batch, const float* const* x, const float* const* f, float* const* y,
+EFF_API int eff_batch_forward_both(const EffBatch* batch, const float* const* x, const float* const* f, float* const* y,
                            void* const* xhat_out, void* const* fhat_out, void* stream);
 /* eff_forward_residual over the batch: r = EFF(x, f) - y_obs per image. */
-int eff_batch_forward_residual(const EffBatch* batch, const float* const* x, const float* const* f,
+EFF_API int eff_batch_forward_residual(const EffBatch* batch, const float* const* x, const float* const* f,
                                const float* const* y_obs, float* const* r, void* const* xhat_out,
                                void* const* fhat_out, void* stream);
 /* eff_adjoint_residual over the batch; y_obs nullable: y is already the
  * residual (eff_batch_forward_residual) and loss (nullable) = 0.5 * sum y^2;
  * gx needs fhat, gf needs xhat. */
-int eff_batch_adjoint_residual(const EffBatch* batch, const float* const* y, const float* const* y_obs,
+EFF_API int eff_batch_adjoint_residual(const EffBatch* batch, const float* const* y, const float* const* y_obs,
                                const void* const* fhat, const void* const* xhat, float* const* gx,
                                float* const* gf, double* const* loss, void* stream);
 
@@ -306,29 +314,29 @@ int eff_batch_adjoint_residual(const EffBatch* batch, const float* const* y, con
  * 0 (default) per call -- a 2-CTA thread-block cluster when one CTA's frame
  * does not fit in shared memory or when twice the grid still fits on the
  * GPU's SMs at once; 1 always one CTA (where it fits); 2 always a cluster. */
-int eff_set_cluster_mode(int mode);
+EFF_API int eff_set_cluster_mode(int mode);
 
 /* Error bits the plan's kernels recorded on the device (EFF_DEVERR_*), read
  * after waiting for all work on the current device; clear != 0 resets them.
  * EFF_DEVERR_COPY_TIMEOUT: a bulk copy into shared memory did not complete
  * within the kernel's wait limit (that call's results are not valid). */
 #define EFF_DEVERR_COPY_TIMEOUT 1
-int eff_plan_device_errors(const EffPlan* plan, int* flags, int clear);
+EFF_API int eff_plan_device_errors(const EffPlan* plan, int* flags, int clear);
 
 /* 1: kernels that multiply by cached spectra (adjoints, forwards from a
  * cached spectrum, deconvolution) copy their columns of the spectra into
  * shared memory with the bulk-copy engine at kernel start, where the CTA's
  * shared memory allows; 0 (default): they read them from global memory,
  * where a step's spectra sit in L2.  For all plans of the process. */
-int eff_set_spectrum_staging(int on);
+EFF_API int eff_set_spectrum_staging(int on);
 
 /* Testing hook: overwrite the device a plan records as its own, so that a
  * test can check that calls on a mismatched device are refused before any
  * work is queued.  Not for production use. */
-int eff_test_plan_set_device(EffPlan* plan, int device);
+EFF_API int eff_test_plan_set_device(EffPlan* plan, int device);
 
 /* Message for the last non-OK status returned on this thread. */
-const char* eff_last_error(void);
+EFF_API const char* eff_last_error(void);
 
 #ifdef __cplusplus
 }

@@ -27,7 +27,12 @@ DEBUG_LIB = os.path.join(OUT_DIR, "libvmbd_eff_debug.so")
 # translation units left out of the debug build (eff_debug_stubs.cu stands in)
 _NOT_IN_DEBUG = ("eff_n192", "eff_n256", "eff_n512", "eff_batch")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
+# hidden visibility: only the C ABI (EFF_API in include/vmbd_eff.h) is exported,
+# so that two builds loaded in one process (the library and its bounds-checked
+# variant) share no symbol -- template statics such as the per-kernel shared
+# memory attribute cache would otherwise be merged across them
+FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2", "-Xcompiler",
+         "-fvisibility=hidden"]
 
 
 def _nvcc() -> str:
