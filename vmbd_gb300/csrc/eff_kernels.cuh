@@ -645,6 +645,13 @@ __device__ __forceinline__ void eff_patch(const Params& P, int k, long long b, f
     if constexpr (CL == 1) __syncthreads();
     else cg::this_cluster().sync();
   };
+  // A cluster barrier that hands over no data (the peers are running / have
+  // finished reading this CTA's frame): relaxed arrive, so that it does not
+  // wait for this CTA's outstanding global stores and atomics.
+  auto cluster_meet = [&]() {
+    if constexpr (CL == 1) __syncthreads();
+    else asm volatile("barrier.cluster.arrive.relaxed.aligned;\n\tbarrier.cluster.wait.aligned;" ::: "memory");
+  };
   // Workers across the cluster for the row passes.
   const int wid = F.rank * NG + gid, NW = CL * NG;
 
@@ -758,7 +765,7 @@ __device__ __forceinline__ void eff_patch(const Params& P, int k, long long b, f
         // The peer must not write into this CTA's frame before it is running
         // (and, in a persistent loop, before this CTA has finished the
         // previous patch).
-        phase_sync();
+        cluster_meet();
         first = false;
       }
       if (row < 0) break;
@@ -846,7 +853,7 @@ __device__ __forceinline__ void eff_patch(const Params& P, int k, long long b, f
   // Spectrum kernels are done; with a cluster, wait for the peer's local
   // column pass so that a following patch cannot write into its frame early.
   if constexpr (OP == OP_SPEC_IMAGE || OP == OP_SPEC_PSF) {
-    if constexpr (CL > 1) phase_sync();
+    if constexpr (CL > 1) cluster_meet();
     return;
   }
   phase_sync();
@@ -1016,7 +1023,7 @@ __device__ __forceinline__ void eff_patch(const Params& P, int k, long long b, f
     }
   }
   // Peers read this CTA's frame in phase 3: stay resident until they finish.
-  if constexpr (CL > 1) phase_sync();
+  if constexpr (CL > 1) cluster_meet();
 }
 
 // Zero the accumulators of the kernel that follows in the same stream (a
