@@ -1,8 +1,8 @@
 // Register / sub-warp FFT building blocks for the EFF kernels (sm_103a).
 //
-// A length-N complex FFT (N = R*G: N = 64, 128, 256 with R = 16 values per
-// lane; N = 192 with R = 24; N = 512 with R = 32) is computed by a group of G
-// consecutive lanes of one warp, each lane holding R values:
+// A length-N complex FFT (N = R*G: N = 64, 256 with R = 16 values per lane;
+// N = 128 with R = 8; N = 192 with R = 24; N = 512 with R = 32) is computed
+// by a group of G consecutive lanes of one warp, each lane holding R values:
 //
 //   layout "A": lane g, register m  <->  element g + G*m.
 //
@@ -156,18 +156,86 @@ __device__ __forceinline__ void dft(float2 (&a)[R]) {
   else dft_pow2<R, INV>(a);
 }
 
-// Values each lane holds for a length-N transform.
-__host__ __device__ constexpr int lane_values(int N) { return N % 3 == 0 ? 24 : (N == 512 ? 32 : 16); }
+// Values each lane holds for a length-N transform (N = 128: 8 values on 16
+// lanes, so that a frame's transforms run on twice as many lanes, each with
+// half the dependent arithmetic).
+__host__ __device__ constexpr int lane_values(int N) {
+  return N % 3 == 0 ? 24 : (N == 512 ? 32 : (N == 128 ? 8 : 16));
+}
+// Exchange scratch (float2) of one lane group: R >= G: one R x (G + 1)
+// transpose; R = G / 2: a R x (G + 2) transpose, then the N outputs with 8
+// padding slots per 64; +8 spreads the groups of a warp over the banks.
+__host__ __device__ constexpr int group_scratch(int N) {
+  return lane_values(N) >= N / lane_values(N)
+             ? lane_values(N) * (N / lane_values(N) + 1) + 8
+             : (lane_values(N) * (N / lane_values(N) + 2) > N + N / 8 ? lane_values(N) * (N / lane_values(N) + 2)
+                                                                      : N + N / 8) +
+                   8;
+}
 
 template <int N>
 struct FftShape {
   static constexpr int R = lane_values(N);          // values per lane
   static constexpr int G = N / R;                    // lanes per transform
-  static constexpr int T = R / G;                    // k1 values per lane after the exchange
-  static constexpr int PAD = 1;                      // scratch row padding (bank spread)
-  static constexpr int SCR = R * (G + PAD) + 8;      // float2 per group scratch (+8: group offset)
-  static_assert(G >= 2 && G <= 16 && (R % G) == 0 && (G & (G - 1)) == 0, "supported N: 32..256, 192, 512");
+  static constexpr int T = R / G;                    // k1 values per lane after the exchange (R >= G)
+  static constexpr int PAD = 1;                      // scratch row padding (bank spread, R >= G)
+  static constexpr int SCR = group_scratch(N);       // float2 per group scratch
+  static_assert(G >= 2 && G <= 16 && ((R % G) == 0 || 2 * R == G) && (G & (G - 1)) == 0,
+                "supported N: 32..512, 192");
 };
+
+// Forward FFT for R = G / 2 (N = 128: 8 values on 16 lanes).  With
+// n = g + G m and k = k1 + R k2: an R-point DFT over m in registers, the
+// twiddle W_N^{g k1}, then for each k1 a G-point DFT over g, which lanes
+// 2 k1 (even g) and 2 k1 + 1 (odd g) share: after a transpose through the
+// scratch each takes an R-point DFT of its half, the odd one twiddles by
+// W_G^{k2}, and one exchange of partners (shuffle) gives the butterfly --
+// the even lane then holds X[k1 + R k2], k2 < R, the odd one k2 >= R.  A
+// second pass through the scratch restores layout A.
+template <int N>
+__device__ __forceinline__ void fft_fwd_half(float2 (&v)[FftShape<N>::R], int g, float2* scr, const float2* tw,
+                                             unsigned mask) {
+  using S = FftShape<N>;
+  constexpr int R = S::R;
+  constexpr int G = S::G;
+  static_assert(2 * R == G, "R = G / 2");
+  constexpr int P1 = G + 2;  // transpose row pitch (conflict-free reads of the odd/even halves)
+  dft<R, false>(v);
+#pragma unroll
+  for (int k1 = 1; k1 < R; ++k1) v[k1] = cmul(v[k1], tw[k1 * G + g]);
+#pragma unroll
+  for (int k1 = 0; k1 < R; ++k1) scr[k1 * P1 + g] = v[k1];
+  __syncwarp(mask);
+  const int p = g >> 1, h = g & 1;
+#pragma unroll
+  for (int j = 0; j < R; ++j) v[j] = scr[p * P1 + 2 * j + h];
+  __syncwarp(mask);
+  dft<R, false>(v);
+  if (h) {
+#pragma unroll
+    for (int k = 1; k < R; ++k) v[k] = twiddle96<false>(v[k], k * (96 / G));  // W_G^k
+  }
+#pragma unroll
+  for (int k = 0; k < R; ++k) {
+    const float ox = __shfl_xor_sync(mask, v[k].x, 1, G);
+    const float oy = __shfl_xor_sync(mask, v[k].y, 1, G);
+    // even lane: E + W O; odd lane: E - W O (its own value is W O)
+    v[k] = h ? make_float2(ox - v[k].x, oy - v[k].y) : make_float2(v[k].x + ox, v[k].y + oy);
+  }
+  // X[p + R (k + R h)] -> the scratch (8 padding slots per 64), layout A back out
+#pragma unroll
+  for (int k = 0; k < R; ++k) {
+    const int n = p + R * k + R * R * h;
+    scr[n + ((n >> 6) << 3)] = v[k];
+  }
+  __syncwarp(mask);
+#pragma unroll
+  for (int m = 0; m < R; ++m) {
+    const int n = g + G * m;
+    v[m] = scr[n + ((n >> 6) << 3)];
+  }
+  __syncwarp(mask);
+}
 
 // Forward FFT of length N over a lane group: v in layout A (natural), out in
 // layout A (natural).  tw: table [k1*G + g] = W_N^{g*k1}.  scr: this group's
@@ -177,6 +245,10 @@ __device__ __forceinline__ void fft_fwd(float2 (&v)[FftShape<N>::R], int g, floa
                                         unsigned mask) {
   using S = FftShape<N>;
   constexpr int R = S::R;
+  if constexpr (R < S::G) {
+    fft_fwd_half<N>(v, g, scr, tw, mask);
+    return;
+  }
   dft<R, false>(v);
 #pragma unroll
   for (int k1 = 1; k1 < R; ++k1) v[k1] = cmul(v[k1], tw[k1 * S::G + g]);
@@ -197,11 +269,20 @@ __device__ __forceinline__ void fft_fwd(float2 (&v)[FftShape<N>::R], int g, floa
 }
 
 // Inverse (unnormalised) FFT: v in layout A (natural frequency), out layout A.
+// (R = G / 2: conj(FFT(conj(v))).)
 template <int N>
 __device__ __forceinline__ void fft_inv(float2 (&v)[FftShape<N>::R], int g, float2* scr, const float2* tw,
                                         unsigned mask) {
   using S = FftShape<N>;
   constexpr int R = S::R;
+  if constexpr (R < S::G) {
+#pragma unroll
+    for (int j = 0; j < R; ++j) v[j].y = -v[j].y;
+    fft_fwd_half<N>(v, g, scr, tw, mask);
+#pragma unroll
+    for (int j = 0; j < R; ++j) v[j].y = -v[j].y;
+    return;
+  }
 #pragma unroll
   for (int t = 0; t < S::T; ++t) {
     float2 w[S::G];

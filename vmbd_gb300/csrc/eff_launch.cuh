@@ -11,7 +11,7 @@ namespace eff {
 // mbarrier.
 inline size_t smem_bytes(int N, int op, const Params& P, int threads, int CL) {
   const int R = lane_values(N), G = N / R;
-  const int scr = R * (G + 1) + 8;
+  const int scr = group_scratch(N);
   size_t n = (size_t)N + (size_t)frame_rows(P, op) * frame_pitch(N, CL) + (size_t)(threads / G) * scr +
              2 * (size_t)N;
   if (const int nst = staged_specs(P, op)) n += 1 + (size_t)nst * staged_cols(N, CL) * (N + kSpecPad) + 1;
