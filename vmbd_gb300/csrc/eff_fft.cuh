@@ -1,8 +1,9 @@
 // Register / sub-warp FFT building blocks for the EFF kernels (sm_103a).
 //
-// A length-N complex FFT (N = R*G: N = 64, 256 with R = 16 values per lane;
-// N = 128 with R = 8; N = 192 with R = 24; N = 512 with R = 32) is computed
-// by a group of G consecutive lanes of one warp, each lane holding R values:
+// A length-N complex FFT (N = R*G: N = 256 with R = 16 values per lane;
+// N = 64, 128 with R = 8; N = 192 with R = 24; N = 512 with R = 32) is
+// computed by a group of G consecutive lanes of one warp, each lane holding R
+// values:
 //
 //   layout "A": lane g, register m  <->  element g + G*m.
 //
@@ -156,11 +157,11 @@ __device__ __forceinline__ void dft(float2 (&a)[R]) {
   else dft_pow2<R, INV>(a);
 }
 
-// Values each lane holds for a length-N transform (N = 128: 8 values on 16
-// lanes, so that a frame's transforms run on twice as many lanes, each with
-// half the dependent arithmetic).
+// Values each lane holds for a length-N transform (N = 64 and 128: 8 values,
+// on 8 and 16 lanes, so that a frame's transforms run on many lanes, each with
+// a short dependent chain).
 __host__ __device__ constexpr int lane_values(int N) {
-  return N % 3 == 0 ? 24 : (N == 512 ? 32 : (N == 128 ? 8 : 16));
+  return N % 3 == 0 ? 24 : (N == 512 ? 32 : (N <= 128 ? 8 : 16));
 }
 // Exchange scratch (float2) of one lane group: R >= G: one R x (G + 1)
 // transpose; R = G / 2: a R x (G + 2) transpose, then the N outputs with 8
