@@ -896,7 +896,10 @@ def main():
                      "peak_kind": hbm_kind, "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic,
                      "algorithmic_bytes": bytes_, "kernel_ms": kern[dom],
                      "fp32": {"ref_alg_tflops": flops / t_dom / 1e12, "peak_tflops_at_clock": fp32_peak,
-                              "frac": flops / t_dom / 1e12 / fp32_peak}},
+                              "frac": flops / t_dom / 1e12 / fp32_peak},
+                     "per_kernel": {k: {"ms": kern[k], "hbm_frac": alg[k][0] / (kern[k] * 1e-3) / 1e9 / hbm,
+                                        "fp32_frac": alg[k][1] / (kern[k] * 1e-3) / 1e12 / fp32_peak}
+                                    for k in kern}},
         "kernels_ms": R["kern_ms"],
         "unfused_gpu": {"ms_per_step": R["unfused_ms"], "value": world * pixels / (R["unfused_ms"] * 1e-3) / 1e6,
                         "speedup": R["unfused_ms"] / R["t_flushed"],
