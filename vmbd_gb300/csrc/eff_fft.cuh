@@ -174,6 +174,21 @@ __host__ __device__ constexpr int group_scratch(int N) {
                    8;
 }
 
+// A lane's twiddle factors W_N^{g k1} held in registers (frame 128: R = 8 of
+// them per lane, loaded once per kernel), or the shared W_N table.
+template <int R>
+struct RegTw {
+  float2 w[R];
+};
+template <int G>
+__device__ __forceinline__ float2 tw_at(const float2* t, int k1, int g) {
+  return t[k1 * G + g];
+}
+template <int G, int R>
+__device__ __forceinline__ float2 tw_at(const RegTw<R>& t, int k1, int) {
+  return t.w[k1];
+}
+
 template <int N>
 struct FftShape {
   static constexpr int R = lane_values(N);          // values per lane
@@ -193,8 +208,8 @@ struct FftShape {
 // W_G^{k2}, and one exchange of partners (shuffle) gives the butterfly --
 // the even lane then holds X[k1 + R k2], k2 < R, the odd one k2 >= R.  A
 // second pass through the scratch restores layout A.
-template <int N>
-__device__ __forceinline__ void fft_fwd_half(float2 (&v)[FftShape<N>::R], int g, float2* scr, const float2* tw,
+template <int N, class TW>
+__device__ __forceinline__ void fft_fwd_half(float2 (&v)[FftShape<N>::R], int g, float2* scr, const TW& tw,
                                              unsigned mask) {
   using S = FftShape<N>;
   constexpr int R = S::R;
@@ -203,7 +218,7 @@ __device__ __forceinline__ void fft_fwd_half(float2 (&v)[FftShape<N>::R], int g,
   constexpr int P1 = G + 2;  // transpose row pitch (conflict-free reads of the odd/even halves)
   dft<R, false>(v);
 #pragma unroll
-  for (int k1 = 1; k1 < R; ++k1) v[k1] = cmul(v[k1], tw[k1 * G + g]);
+  for (int k1 = 1; k1 < R; ++k1) v[k1] = cmul(v[k1], tw_at<G>(tw, k1, g));
 #pragma unroll
   for (int k1 = 0; k1 < R; ++k1) scr[k1 * P1 + g] = v[k1];
   __syncwarp(mask);
@@ -241,8 +256,8 @@ __device__ __forceinline__ void fft_fwd_half(float2 (&v)[FftShape<N>::R], int g,
 // Forward FFT of length N over a lane group: v in layout A (natural), out in
 // layout A (natural).  tw: table [k1*G + g] = W_N^{g*k1}.  scr: this group's
 // scratch (FftShape<N>::SCR float2).  mask: the group's lanes.
-template <int N>
-__device__ __forceinline__ void fft_fwd(float2 (&v)[FftShape<N>::R], int g, float2* scr, const float2* tw,
+template <int N, class TW>
+__device__ __forceinline__ void fft_fwd(float2 (&v)[FftShape<N>::R], int g, float2* scr, const TW& tw,
                                         unsigned mask) {
   using S = FftShape<N>;
   constexpr int R = S::R;
@@ -252,7 +267,7 @@ __device__ __forceinline__ void fft_fwd(float2 (&v)[FftShape<N>::R], int g, floa
   }
   dft<R, false>(v);
 #pragma unroll
-  for (int k1 = 1; k1 < R; ++k1) v[k1] = cmul(v[k1], tw[k1 * S::G + g]);
+  for (int k1 = 1; k1 < R; ++k1) v[k1] = cmul(v[k1], tw_at<S::G>(tw, k1, g));
 #pragma unroll
   for (int k1 = 0; k1 < R; ++k1) scr[k1 * (S::G + S::PAD) + g] = v[k1];
   __syncwarp(mask);
@@ -271,8 +286,8 @@ __device__ __forceinline__ void fft_fwd(float2 (&v)[FftShape<N>::R], int g, floa
 
 // Inverse (unnormalised) FFT: v in layout A (natural frequency), out layout A.
 // (R = G / 2: conj(FFT(conj(v))).)
-template <int N>
-__device__ __forceinline__ void fft_inv(float2 (&v)[FftShape<N>::R], int g, float2* scr, const float2* tw,
+template <int N, class TW>
+__device__ __forceinline__ void fft_inv(float2 (&v)[FftShape<N>::R], int g, float2* scr, const TW& tw,
                                         unsigned mask) {
   using S = FftShape<N>;
   constexpr int R = S::R;
@@ -299,7 +314,7 @@ __device__ __forceinline__ void fft_inv(float2 (&v)[FftShape<N>::R], int g, floa
   for (int k1 = 0; k1 < R; ++k1) v[k1] = scr[k1 * (S::G + S::PAD) + g];
   __syncwarp(mask);
 #pragma unroll
-  for (int k1 = 1; k1 < R; ++k1) v[k1] = cmulc(v[k1], tw[k1 * S::G + g]);
+  for (int k1 = 1; k1 < R; ++k1) v[k1] = cmulc(v[k1], tw_at<S::G>(tw, k1, g));
   dft<R, true>(v);
 }
 

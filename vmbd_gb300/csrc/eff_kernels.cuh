@@ -370,9 +370,9 @@ __device__ __forceinline__ void load_rows(const Params& P, const Patch& T, int r
 // R2C of one pair of rows already in v (layout A), first half: the packed
 // transform in v and its Hermitian partners in p (registers only, no frame
 // access, so it may run before the cluster's CTAs are known to be running).
-template <int N>
+template <int N, class TW>
 __device__ __forceinline__ void r2c_transform(float2 (&v)[FftShape<N>::R], float2 (&p)[FftShape<N>::R], float2* scr,
-                                              const float2* tw, int g, unsigned gmask) {
+                                              const TW& tw, int g, unsigned gmask) {
   fft_fwd<N>(v, g, scr, tw, gmask);
   hermitian_partner<N>(v, p, g, gmask);
 }
@@ -406,9 +406,9 @@ __device__ __forceinline__ void r2c_scatter(const float2 (&v)[FftShape<N>::R], c
 
 // C2R of frame rows (ra, ra+1); returns real row ra in .x, ra+1 in .y,
 // layout A (register m holds column g + G*m).
-template <int N, int CL>
+template <int N, int CL, class TW>
 __device__ __forceinline__ void c2r_unit(const Frame<N, CL>& F, int ra, float2 (&v)[FftShape<N>::R], float2* scr,
-                                         const float2* tw, int g, unsigned gmask) {
+                                         const TW& tw, int g, unsigned gmask) {
   constexpr int G = FftShape<N>::G;
   constexpr int R = FftShape<N>::R;
   constexpr int HP = Frame<N, CL>::HP;
@@ -621,7 +621,7 @@ __device__ __forceinline__ void eff_patch(const Params& P, int k, long long b, f
   constexpr int R = FftShape<N>::R;
   constexpr int A = opnd_a(OP);
   constexpr int HP = frame_pitch(N, CL);
-  float2* tw = smem;         // N entries
+  float2* tw_s = smem;       // N entries (the W_N table; frame 128 keeps each lane's factors in registers)
   float2* frame = smem + N;  // frame_rows(P, OP) * HP
   const int tid = threadIdx.x;
   const int NG = blockDim.x / G;
@@ -684,9 +684,24 @@ __device__ __forceinline__ void eff_patch(const Params& P, int k, long long b, f
   stage += (reinterpret_cast<unsigned long long>(stage) & 15ull) ? 1 : 0;
   unsigned long long* sbar = reinterpret_cast<unsigned long long*>(stage + nst * SC * SP);
 
-  for (int i = tid; i < N; i += blockDim.x) tw[i] = __ldg(P.tw + i);
+  // Twiddles: R < G (frame 128) -- this lane's R factors W_N^{g k1} in
+  // registers, loaded here with no barrier before the first transform; else
+  // the W_N table in shared memory.
+  constexpr bool kRegTw = R < G;
+  const auto tw = [&]() {
+    if constexpr (kRegTw) {
+      RegTw<R> t;
+#pragma unroll
+      for (int k1 = 0; k1 < R; ++k1) t.w[k1] = __ldg(P.tw + k1 * G + g);
+      return t;
+    } else {
+      return static_cast<const float2*>(tw_s);
+    }
+  }();
+  if constexpr (!kRegTw)
+    for (int i = tid; i < N; i += blockDim.x) tw_s[i] = __ldg(P.tw + i);
   if (nst && tid == 0) mbar_init(sbar, 1);
-  __syncthreads();  // the twiddles (and the mbarrier), before the first use
+  if (!kRegTw || nst) __syncthreads();  // the twiddle table / the mbarrier, before the first use
   // Cached spectra this CTA multiplies by in the column pass: its columns of
   // each, copied into shared memory by the bulk-copy engine while the row
   // pass runs (one column per copy, into padded slots).
