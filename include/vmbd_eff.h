@@ -73,9 +73,9 @@ typedef struct EffGeom {
   int hop[2];  /* patch hop */
   int sfft;    /* FFT frame edge, 64, 128, 192, 256 or 512 (>= max(E)); 0 = the smallest power of two >= max(E) */
   int mode;    /* EFF_MODE_* */
-  int threads; /* CTA size, a multiple of 32 up to the frame's maximum (512; 384 for frame
-                  192, 576 for 256, 256 for 512); 0 = the largest that fits.  Lowered to
-                  fit shared memory. */
+  int threads; /* CTA size, a multiple of 32 up to the frame's maximum (512 for frame 64,
+                  544 for 128, 384 for 192, 576 for 256, 256 for 512); 0 = the largest that
+                  fits.  Lowered to fit shared memory. */
   int flags;   /* EFF_GEOM_* */
 } EffGeom;
 

@@ -684,10 +684,10 @@ __device__ __forceinline__ void eff_patch(const Params& P, int k, long long b, f
   stage += (reinterpret_cast<unsigned long long>(stage) & 15ull) ? 1 : 0;
   unsigned long long* sbar = reinterpret_cast<unsigned long long*>(stage + nst * SC * SP);
 
-  // Twiddles: R < G (frame 128) -- this lane's R factors W_N^{g k1} in
-  // registers, loaded here with no barrier before the first transform; else
-  // the W_N table in shared memory.
-  constexpr bool kRegTw = R < G;
+  // Twiddles: R = 8 (frames 64 and 128) -- this lane's R factors
+  // W_N^{g k1} in registers, loaded here with no barrier before the first
+  // transform; else the W_N table in shared memory.
+  constexpr bool kRegTw = R <= 8;
   const auto tw = [&]() {
     if constexpr (kRegTw) {
       RegTw<R> t;
