@@ -1,9 +1,8 @@
 // Register / sub-warp FFT building blocks for the EFF kernels (sm_103a).
 //
-// A length-N complex FFT (N = R*G: N = 256 with R = 16 values per lane;
-// N = 64, 128 with R = 8; N = 192 with R = 24; N = 512 with R = 32) is
-// computed by a group of G consecutive lanes of one warp, each lane holding R
-// values:
+// A length-N complex FFT (N = R*G: N = 256, 512 with R = 16 values per lane;
+// N = 64, 128 with R = 8; N = 192 with R = 24) is computed by a group of G
+// consecutive lanes of one warp, each lane holding R values:
 //
 //   layout "A": lane g, register m  <->  element g + G*m.
 //
@@ -161,16 +160,17 @@ __device__ __forceinline__ void dft(float2 (&a)[R]) {
 // on 8 and 16 lanes, so that a frame's transforms run on many lanes, each with
 // a short dependent chain).
 __host__ __device__ constexpr int lane_values(int N) {
-  return N % 3 == 0 ? 24 : (N == 512 ? 32 : (N <= 128 ? 8 : 16));
+  return N % 3 == 0 ? 24 : (N <= 128 ? 8 : 16);
 }
 // Exchange scratch (float2) of one lane group: R >= G: one R x (G + 1)
 // transpose; R = G / 2: a R x (G + 2) transpose, then the N outputs with 8
-// padding slots per 64; +8 spreads the groups of a warp over the banks.
+// padding slots per R*R; +8 spreads the groups of a warp over the banks.
 __host__ __device__ constexpr int group_scratch(int N) {
   return lane_values(N) >= N / lane_values(N)
              ? lane_values(N) * (N / lane_values(N) + 1) + 8
-             : (lane_values(N) * (N / lane_values(N) + 2) > N + N / 8 ? lane_values(N) * (N / lane_values(N) + 2)
-                                                                      : N + N / 8) +
+             : (lane_values(N) * (N / lane_values(N) + 2) > N + 8 * (N / (lane_values(N) * lane_values(N)))
+                    ? lane_values(N) * (N / lane_values(N) + 2)
+                    : N + 8 * (N / (lane_values(N) * lane_values(N)))) +
                    8;
 }
 
@@ -196,11 +196,12 @@ struct FftShape {
   static constexpr int T = R / G;                    // k1 values per lane after the exchange (R >= G)
   static constexpr int PAD = 1;                      // scratch row padding (bank spread, R >= G)
   static constexpr int SCR = group_scratch(N);       // float2 per group scratch
-  static_assert(G >= 2 && G <= 16 && ((R % G) == 0 || 2 * R == G) && (G & (G - 1)) == 0,
+  static_assert(G >= 2 && G <= 32 && ((R % G) == 0 || 2 * R == G) && (G & (G - 1)) == 0,
                 "supported N: 32..512, 192");
 };
 
-// Forward FFT for R = G / 2 (N = 128: 8 values on 16 lanes).  With
+// Forward FFT for R = G / 2 (N = 128: 8 values on 16 lanes; N = 512: 16
+// values on 32 lanes).  With
 // n = g + G m and k = k1 + R k2: an R-point DFT over m in registers, the
 // twiddle W_N^{g k1}, then for each k1 a G-point DFT over g, which lanes
 // 2 k1 (even g) and 2 k1 + 1 (odd g) share: after a transpose through the
@@ -238,17 +239,18 @@ __device__ __forceinline__ void fft_fwd_half(float2 (&v)[FftShape<N>::R], int g,
     // even lane: E + W O; odd lane: E - W O (its own value is W O)
     v[k] = h ? make_float2(ox - v[k].x, oy - v[k].y) : make_float2(v[k].x + ox, v[k].y + oy);
   }
-  // X[p + R (k + R h)] -> the scratch (8 padding slots per 64), layout A back out
+  // X[p + R (k + R h)] -> the scratch (8 padding slots per R*R, so that the
+  // two halves h of a half-warp land on different banks), layout A back out
 #pragma unroll
   for (int k = 0; k < R; ++k) {
     const int n = p + R * k + R * R * h;
-    scr[n + ((n >> 6) << 3)] = v[k];
+    scr[n + (n / (R * R)) * 8] = v[k];
   }
   __syncwarp(mask);
 #pragma unroll
   for (int m = 0; m < R; ++m) {
     const int n = g + G * m;
-    v[m] = scr[n + ((n >> 6) << 3)];
+    v[m] = scr[n + (n / (R * R)) * 8];
   }
   __syncwarp(mask);
 }

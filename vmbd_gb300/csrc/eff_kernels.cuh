@@ -152,7 +152,7 @@ __host__ __device__ constexpr int frame_pitch(int N, int CL = 1) { return CL == 
 __host__ __device__ constexpr int even_up(int v) { return (v + 1) & ~1; }
 // Threads per CTA the kernel is compiled for (the host may launch fewer).
 __host__ __device__ constexpr int max_threads(int N) {
-  return N % 3 == 0 ? 384 : (N == 256 ? 576 : (N == 512 ? 256 : (N == 128 ? 544 : 512)));
+  return N % 3 == 0 ? 384 : (N == 256 ? 576 : (N == 128 ? 544 : 512));
 }
 
 // Operand A / B of each op, their row counts and frame bases.
