@@ -426,7 +426,8 @@ def kernel_times(plan, sets, r, xhat, fhat, gx, gf, loss, stream, dev, reps):
                                              _ptr(fhat), _lib.OUT_ZEROED, _ptr(gx), nx, _ptr(loss), 1, 1, st))
         if n >= 2:
             _lib.check(L.eff_adjoint_ex(plan._h, _ptr(r), None, None, _ptr(fhat), _ptr(xhat), _ptr(gx), _ptr(gf),
-                                        _ptr(loss), _lib.ADJ_EXACT, _lib.OUT_ZEROED | _lib.LOSS_OF_Y, 1, st))
+                                        _ptr(loss), _lib.ADJ_EXACT,
+                                        _lib.OUT_ZEROED | _lib.LOSS_OF_Y | _lib.AFTER_FORWARD, 1, st))
 
     graphs = [[], [], []]
     with torch.cuda.stream(stream):

@@ -58,6 +58,9 @@ extern "C" {
 
 #define EFF_OUT_ZEROED 1 /* flags: the call's accumulated output is already zero (no memset) */
 #define EFF_LOSS_OF_Y 2  /* eff_adjoint_ex flags: y is already a residual; loss += 0.5 * sum y^2 */
+#define EFF_AFTER_FORWARD 4 /* eff_adjoint_ex flags: the call directly follows, on the same stream,
+                               the forward call that produced its inputs; its kernel may be
+                               scheduled while that one runs and waits for it on the device */
 
 #define EFF_OPERAND_IMAGE 0 /* eff_forward_ex: u is the image, spec the PSF spectrum */
 #define EFF_OPERAND_PSF 1   /* eff_forward_ex: u is the PSF stack, spec the image spectrum */
@@ -236,7 +239,9 @@ EFF_API int eff_adjoint_masked(const EffPlan* plan, const float* y, const float*
  * eff_adjoint_ex: eff_adjoint / eff_adjoint_residual (y_obs) /
  *   eff_adjoint_masked (mask) in one; flags EFF_OUT_ZEROED: gx and loss are
  *   already zero; EFF_LOSS_OF_Y (no y_obs, no mask): y is the residual, as
- *   eff_forward_residual leaves it, and loss (nullable) += 0.5 * sum y^2. */
+ *   eff_forward_residual leaves it, and loss (nullable) += 0.5 * sum y^2;
+ *   EFF_AFTER_FORWARD: programmatic dependent launch after the preceding
+ *   forward call (eff_loss_grad does this internally). */
 EFF_API int eff_forward_ex(const EffPlan* plan, int operand, const float* u, const void* spec, float* y, const float* sub,
                    void* spec_out, int flags, float* zero_f, long long zero_nf, double* zero_d, int zero_nd,
                    int batch, void* stream);

@@ -479,4 +479,14 @@ def test_chained_call_entry_points(cuda):
     assert L.eff_forward_ex(plan._h, _lib.OPERAND_IMAGE, _ptr(xt), _ptr(fh), _ptr(y_img), _ptr(y_img), None, 0,
                             None, 0, None, 0, 1, st) == _lib.EFF_ERR_INVALID
     assert L.eff_adjoint_ex(plan._h, _ptr(rt), None, None, _ptr(fh), None, _ptr(gx_ref), None, None,
-                            _lib.ADJ_EXACT, 4, 1, st) == _lib.EFF_ERR_INVALID
+                            _lib.ADJ_EXACT, 8, 1, st) == _lib.EFF_ERR_INVALID
+    # EFF_AFTER_FORWARD: the adjoint launched to overlap the forward it follows
+    # (it waits for the forward's results on the device) gives the same output
+    res = torch.zeros_like(y_img)
+    _lib.check(L.eff_forward_ex(plan._h, _lib.OPERAND_IMAGE, _ptr(xt), _ptr(fh), _ptr(res), _ptr(rt), None,
+                                _lib.OUT_ZEROED, None, 0, None, 0, 1, st))
+    gx_pdl = torch.full(plan.sx, 3.0, device=cuda)
+    _lib.check(L.eff_adjoint_ex(plan._h, _ptr(res), None, None, _ptr(fh), None, _ptr(gx_pdl), None, None,
+                                _lib.ADJ_EXACT, _lib.AFTER_FORWARD, 1, st))
+    gx_plain, _ = plan.adjoint(res, fh, xh, want_psf=False)
+    assert rel(gx_pdl.cpu(), gx_plain.cpu()) < 1e-6

@@ -20,6 +20,7 @@ ADJ_EXACT = 0
 ADJ_REFERENCE = 1
 OUT_ZEROED = 1
 LOSS_OF_Y = 2
+AFTER_FORWARD = 4
 OPERAND_IMAGE = 0
 OPERAND_PSF = 1
 GEOM_DETERMINISTIC = 1

@@ -266,7 +266,8 @@ int check_plan(const EffPlan* p, int batch) {
 // zeroed: gx and loss were already zeroed on the stream (by the fused forward).
 int adjoint_impl(const EffPlan* plan, const float* y, const float* y_obs, const void* fhat,
                  const void* xhat, float* gx, float* gf, double* loss, int adj_mode, int batch,
-                 void* stream, const float* mask = nullptr, bool zeroed = false, bool loss_y = false) {
+                 void* stream, const float* mask = nullptr, bool zeroed = false, bool loss_y = false,
+                 bool after_forward = false) {
   if (int s = check_plan(plan, batch)) return s;
   if (!y || (!gx && !gf)) return fail(EFF_ERR_INVALID, "null argument");
   if (gx && !fhat) return fail(EFF_ERR_INVALID, "image adjoint needs the PSF spectrum");
@@ -285,6 +286,7 @@ int adjoint_impl(const EffPlan* plan, const float* y, const float* y_obs, const 
   P.out1 = gf;
   P.loss = loss;
   P.loss_y = loss_y ? 1 : 0;
+  P.pdl = after_forward ? 1 : 0;
   P.out0_bs = P.x_bs;
   P.out1_bs = P.f_bs;
   if (adj_mode == EFF_ADJ_REFERENCE) {
@@ -357,8 +359,9 @@ int loss_grad_impl(const EffPlan* plan, const float* x, const float* f, const fl
   if (e != cudaSuccess) return cuda_fail(e, "clearing an output");
   int s = run(plan, eff::OP_FWD_BOTH, P, batch, stream);
   if (s != EFF_OK) return s;
+  // the adjoint may be scheduled while the forward runs (it waits for it)
   return adjoint_impl(plan, y, nullptr, gx ? fhat : nullptr, gf ? xhat : nullptr, gx, gf, loss,
-                      EFF_ADJ_EXACT, batch, stream, nullptr, true, true);
+                      EFF_ADJ_EXACT, batch, stream, nullptr, true, true, true);
 }
 
 }  // namespace
@@ -667,12 +670,12 @@ int eff_forward_ex(const EffPlan* plan, int operand, const float* u, const void*
 int eff_adjoint_ex(const EffPlan* plan, const float* y, const float* y_obs, const float* mask, const void* fhat,
                    const void* xhat, float* gx, float* gf, double* loss, int adj_mode, int flags, int batch,
                    void* stream) {
-  if (flags & ~(EFF_OUT_ZEROED | EFF_LOSS_OF_Y)) return fail(EFF_ERR_INVALID, "flags");
+  if (flags & ~(EFF_OUT_ZEROED | EFF_LOSS_OF_Y | EFF_AFTER_FORWARD)) return fail(EFF_ERR_INVALID, "flags");
   const bool loss_y = (flags & EFF_LOSS_OF_Y) != 0;
   if (loss_y && (y_obs || mask)) return fail(EFF_ERR_INVALID, "EFF_LOSS_OF_Y takes no y_obs or mask");
   if (loss && !y_obs && !loss_y) return fail(EFF_ERR_INVALID, "the loss needs y_obs (or EFF_LOSS_OF_Y)");
   return adjoint_impl(plan, y, y_obs, fhat, xhat, gx, gf, loss, adj_mode, batch, stream, mask,
-                      (flags & EFF_OUT_ZEROED) != 0, loss_y);
+                      (flags & EFF_OUT_ZEROED) != 0, loss_y, (flags & EFF_AFTER_FORWARD) != 0);
 }
 
 int eff_adjoint(const EffPlan* plan, const float* y, const void* fhat, const void* xhat, float* gx,

@@ -265,25 +265,25 @@ __device__ __forceinline__ void fft_fwd(float2 (&v)[FftShape<N>::R], int g, floa
   constexpr int R = S::R;
   if constexpr (R < S::G) {
     fft_fwd_half<N>(v, g, scr, tw, mask);
-    return;
+  } else {
+    dft<R, false>(v);
+#pragma unroll
+    for (int k1 = 1; k1 < R; ++k1) v[k1] = cmul(v[k1], tw_at<S::G>(tw, k1, g));
+#pragma unroll
+    for (int k1 = 0; k1 < R; ++k1) scr[k1 * (S::G + S::PAD) + g] = v[k1];
+    __syncwarp(mask);
+#pragma unroll
+    for (int t = 0; t < S::T; ++t) {
+      float2 w[S::G];
+      const int k1 = g + S::G * t;
+#pragma unroll
+      for (int n2 = 0; n2 < S::G; ++n2) w[n2] = scr[k1 * (S::G + S::PAD) + n2];
+      dft<S::G, false>(w);
+#pragma unroll
+      for (int k2 = 0; k2 < S::G; ++k2) v[t + S::T * k2] = w[k2];
+    }
+    __syncwarp(mask);
   }
-  dft<R, false>(v);
-#pragma unroll
-  for (int k1 = 1; k1 < R; ++k1) v[k1] = cmul(v[k1], tw_at<S::G>(tw, k1, g));
-#pragma unroll
-  for (int k1 = 0; k1 < R; ++k1) scr[k1 * (S::G + S::PAD) + g] = v[k1];
-  __syncwarp(mask);
-#pragma unroll
-  for (int t = 0; t < S::T; ++t) {
-    float2 w[S::G];
-    const int k1 = g + S::G * t;
-#pragma unroll
-    for (int n2 = 0; n2 < S::G; ++n2) w[n2] = scr[k1 * (S::G + S::PAD) + n2];
-    dft<S::G, false>(w);
-#pragma unroll
-    for (int k2 = 0; k2 < S::G; ++k2) v[t + S::T * k2] = w[k2];
-  }
-  __syncwarp(mask);
 }
 
 // Inverse (unnormalised) FFT: v in layout A (natural frequency), out layout A.
@@ -299,25 +299,25 @@ __device__ __forceinline__ void fft_inv(float2 (&v)[FftShape<N>::R], int g, floa
     fft_fwd_half<N>(v, g, scr, tw, mask);
 #pragma unroll
     for (int j = 0; j < R; ++j) v[j].y = -v[j].y;
-    return;
+  } else {
+#pragma unroll
+    for (int t = 0; t < S::T; ++t) {
+      float2 w[S::G];
+#pragma unroll
+      for (int k2 = 0; k2 < S::G; ++k2) w[k2] = v[t + S::T * k2];
+      dft<S::G, true>(w);
+      const int k1 = g + S::G * t;
+#pragma unroll
+      for (int n2 = 0; n2 < S::G; ++n2) scr[k1 * (S::G + S::PAD) + n2] = w[n2];
+    }
+    __syncwarp(mask);
+#pragma unroll
+    for (int k1 = 0; k1 < R; ++k1) v[k1] = scr[k1 * (S::G + S::PAD) + g];
+    __syncwarp(mask);
+#pragma unroll
+    for (int k1 = 1; k1 < R; ++k1) v[k1] = cmulc(v[k1], tw_at<S::G>(tw, k1, g));
+    dft<R, true>(v);
   }
-#pragma unroll
-  for (int t = 0; t < S::T; ++t) {
-    float2 w[S::G];
-#pragma unroll
-    for (int k2 = 0; k2 < S::G; ++k2) w[k2] = v[t + S::T * k2];
-    dft<S::G, true>(w);
-    const int k1 = g + S::G * t;
-#pragma unroll
-    for (int n2 = 0; n2 < S::G; ++n2) scr[k1 * (S::G + S::PAD) + n2] = w[n2];
-  }
-  __syncwarp(mask);
-#pragma unroll
-  for (int k1 = 0; k1 < R; ++k1) v[k1] = scr[k1 * (S::G + S::PAD) + g];
-  __syncwarp(mask);
-#pragma unroll
-  for (int k1 = 1; k1 < R; ++k1) v[k1] = cmulc(v[k1], tw_at<S::G>(tw, k1, g));
-  dft<R, true>(v);
 }
 
 // Value of register j's Hermitian partner: X[N - (g + G*j)] from the lane

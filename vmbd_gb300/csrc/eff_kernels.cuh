@@ -85,6 +85,8 @@ struct Params {
                            //   tiles + (b K + k) * tile size, instead of adding it into the image;
                            //   ola_gather sums the tiles in a fixed order
   double* loss_part;       // deterministic loss: each CTA stores its share at loss_part[b ncta + cta]
+  int pdl;                 // launched with programmatic stream serialization right after the
+                           //   kernel whose results it reads: wait (griddepcontrol.wait) first
 };
 
 // TMA bulk prefetch of a contiguous range into L2 (16-byte aligned start and
@@ -698,6 +700,13 @@ __device__ __forceinline__ void eff_patch(const Params& P, int k, long long b, f
       return static_cast<const float2*>(tw_s);
     }
   }();
+  // A forward lets the kernel after it (the adjoint of a loss/gradient step)
+  // be scheduled now, onto SMs this grid leaves free; a kernel launched that
+  // way waits here until its predecessor has finished and its results are
+  // visible, before it reads anything that kernel wrote.
+  if constexpr (OP == OP_FWD_BOTH || OP == OP_FWD_IMAGE || OP == OP_FWD_PSF)
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  if (P.pdl) asm volatile("griddepcontrol.wait;" ::: "memory");
   if constexpr (!kRegTw)
     for (int i = tid; i < N; i += blockDim.x) tw_s[i] = __ldg(P.tw + i);
   if (nst && tid == 0) mbar_init(sbar, 1);

@@ -33,24 +33,29 @@ cudaError_t launch_one(const Params& P, int K, int batch, int threads, size_t sm
     if (e != cudaSuccess) return e;
     if (dev < 64) attr_bytes[dev].store((int)smem);
   }
-  if constexpr (CL == 1) {
-    kern<<<dim3(K, batch), threads, smem, st>>>(P);
-  } else {
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(K * CL, batch);
-    cfg.blockDim = dim3(threads);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = st;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = CL;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    e = cudaLaunchKernelEx(&cfg, kern, P);
-    if (e != cudaSuccess) return e;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(K * CL, batch);
+  cfg.blockDim = dim3(threads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[2];
+  int na = 0;
+  if (CL > 1) {
+    attr[na].id = cudaLaunchAttributeClusterDimension;
+    attr[na].val.clusterDim.x = CL;
+    attr[na].val.clusterDim.y = 1;
+    attr[na].val.clusterDim.z = 1;
+    ++na;
   }
+  if (P.pdl) {  // may start while its predecessor on the stream runs; waits before reading
+    attr[na].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[na].val.programmaticStreamSerializationAllowed = 1;
+    ++na;
+  }
+  cfg.attrs = attr;
+  cfg.numAttrs = na;
+  e = cudaLaunchKernelEx(&cfg, kern, P);
+  if (e != cudaSuccess) return e;
   return cudaGetLastError();
 }
 

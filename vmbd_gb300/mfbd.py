@@ -128,8 +128,9 @@ class OnlineMFBD:
                                      _ptr(self.y), None, OZ if k > 0 else 0, _ptr(self.yg) if k == 0 else None,
                                      ny if k == 0 else 0, _ptr(self.dots), 3, 1, st))
         # g = X^T (X f - y); the BB / exact-line-search steps need no objective value
+        # (launched to overlap the forward's tail; it waits for the forward)
         self._check(L.eff_adjoint_ex(P._h, _ptr(self.ypred), None, None, None, _ptr(self.xhat),
-                                     None, _ptr(self.g), None, amode, 0, 1, st))
+                                     None, _ptr(self.g), None, amode, _lib.AFTER_FORWARD, 1, st))
         if k == 0:
             self._check(L.eff_forward_ex(P._h, _lib.OPERAND_PSF, _ptr(self.g), _ptr(self.xhat),
                                          _ptr(self.yg), None, None, OZ, None, 0, None, 0, 1, st))
@@ -167,7 +168,7 @@ class OnlineMFBD:
                                      _ptr(self.ypred), None, None, OZ if (i > 0 or self.n_pg > 0) else 0,
                                      _ptr(self._denx), nx + 1, None, 0, 1, st))
         self._check(L.eff_adjoint_ex(P._h, _ptr(self.ypred), None, _ptr(self.mask), _ptr(self.fhat), None,
-                                     _ptr(self.den), None, None, amode, OZ, 1, st))
+                                     _ptr(self.den), None, None, amode, OZ | _lib.AFTER_FORWARD, 1, st))
         last = i == self.n_mu - 1
         self._check(L.eff_mu_update(_ptr(self.x), _ptr(self.num), _ptr(self.den),
                                     ctypes.c_float(self.tol), self.sx[0], self.sx[1], self.sf[0],
