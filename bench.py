@@ -9,17 +9,20 @@ spectrum, fused forward (which also leaves the windowed-patch spectrum),
 residual, fused adjoint giving both gradients.  Metric: image Mpixel/s of
 that step.  Inputs are seeded synthetic data (no dataset is distributed).
 
-``value``: device-resident inputs, the step captured in a CUDA graph, per-step
-CUDA events summed; the timed steps rotate through distinct input sets of over
-twice the L2 in total, so each step reads inputs from HBM (``l2_flushed``:
-the same step after a 256 MB write instead, which also evicts the kernels'
-code).
+``value``: device-resident inputs, the step captured in a CUDA graph, the K
+timed steps replayed back to back between two CUDA events; the timed steps
+rotate through distinct input sets of over twice the L2 in total, so each
+step reads inputs from HBM (``per_step_events``: the sum of each step's own
+event interval instead; ``l2_flushed``: the step after a 256 MB write, which
+also evicts the kernels' code).
 ``e2e``: the same step through the public API from pinned host buffers
 (rotating through as many distinct host input sets), with the host->device
 copy of (x, f, y_obs) and the device->host copy of (gx, gf, loss) of every
 image inside the timed region, for a stream of images: two buffer pairs and
 copy streams, so that the copies of neighbouring images overlap the step
-(``e2e.one_at_a_time``: copy in, step, copy out, then the next image).
+(``e2e.one_at_a_time``: copy in, step, copy out, then the next image).  The
+copies and the step of an image are captured in one CUDA graph (memcpy nodes
+and the step's kernels), one replay per image.
 ``--impl reference``: the FP64 oracle port of the reference algorithm on the
 host cores (scipy.fft over all cores), same workload.
 
@@ -219,7 +222,15 @@ def run_ours(args, rank, world, dev):
         torch.cuda.synchronize(dev)
 
         def timed_graph(n, flushed=False):
+            """(sum of the steps' own event intervals, whole loop) in ms.
+            The whole loop -- n steps replayed back to back, as a job over a
+            stream of images runs them -- is the throughput figure; the sum
+            of per-step intervals also charges every replay's launch latency
+            (a loop that waits for each step's result sees about that)."""
             evs = []
+            a0 = torch.cuda.Event(enable_timing=True)
+            b0 = torch.cuda.Event(enable_timing=True)
+            a0.record(stream)
             for k in range(n):
                 if flushed:
                     flush.fill_(1.0)
@@ -229,28 +240,29 @@ def run_ours(args, rank, world, dev):
                 (graph if flushed else graphs[k % POOL]).replay()
                 b.record(stream)
                 evs.append((a, b))
+            b0.record(stream)
             torch.cuda.synchronize(dev)
-            return sum(a.elapsed_time(b) for a, b in evs)
+            return sum(a.elapsed_time(b) for a, b in evs), a0.elapsed_time(b0)
 
         timed_graph(max(args.warmup, POOL))  # every set once, so that the timed steps see a steady state
         clocks = Clocks(dev.index if dev.index is not None else 0)
         barrier(world)
         torch.cuda.synchronize(dev)
         clocks.start()
-        t_ms = timed_graph(args.steps)
+        t_events, t_ms = timed_graph(args.steps)
         torch.cuda.synchronize(dev)
         barrier(world)
         clk = clocks.stop()
         t_ms = allreduce_max(t_ms, world, dev)
+        t_events = allreduce_max(t_events, world, dev)
         # the same step with the L2 flushed before it (one set): data and the
-        # kernels' code are then read from HBM
+        # kernels' code are then read from HBM (per-step intervals: the loop
+        # also holds the flushes)
         timed_graph(args.warmup, flushed=True)
-        t_flushed = timed_graph(args.steps, flushed=True) / args.steps
+        t_flushed = timed_graph(args.steps, flushed=True)[0] / args.steps
 
-        # per-kernel durations inside the step: the step's own sequence (memset
-        # of the residual, the fused residual forward clearing the adjoint's
-        # accumulators as a side job, the fused adjoint) captured with timing
-        # events between its kernels, L2 flushed before each replay
+        # per-kernel durations inside the step: differences of graph-captured
+        # prefixes of the step's own sequence, input sets rotated
         kern_ms = kernel_times(plan, sets, y, xhat, fhat, gx, gf, loss, stream, dev,
                                reps=max(5, min(args.steps, 50)))
 
@@ -312,83 +324,91 @@ def run_ours(args, rank, world, dev):
                 ut += a.elapsed_time(b)
         unfused_ms = ut / args.steps
 
-        # end to end through the public API from pinned host buffers: the
-        # step's inputs in one host->device copy, its outputs in one
-        # device->host copy
-        # a stream of distinct images from pinned host memory (POOL sets,
-        # over twice the L2 in total)
+        # End to end through the public API from pinned host buffers: per
+        # image, one host->device copy of its inputs (x, f, y_obs) from a
+        # rotating pool of distinct pinned host sets (over twice the L2), the
+        # step, one device->host copy of its outputs (gx, gf, loss).  The
+        # copies and the step are captured in CUDA graphs (memcpy nodes + the
+        # step's kernels), one replay per image, so that the host's speed at
+        # issuing calls does not set the number.
         hins = pool.cpu().pin_memory()
         hout = torch.empty(outbuf.shape, dtype=torch.uint8).pin_memory()
+        s_in = torch.cuda.Stream(device=dev)
+        s_out = torch.cuda.Stream(device=dev)
 
-        def e2e_step(k):
-            inbuf.copy_(hins[k % POOL], non_blocking=True)
-            graph.replay()
-            hout.copy_(outbuf, non_blocking=True)
-
-        # (1) one call at a time: copy in, step, copy out, then the next
+        # (1) one image at a time: copy in, step, copy out, then the next
+        one = []
+        for k in range(POOL):
+            g1 = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g1, stream=stream):
+                inbuf.copy_(hins[k], non_blocking=True)
+                step()
+                hout.copy_(outbuf, non_blocking=True)
+            one.append(g1)
+        torch.cuda.synchronize(dev)
         for k in range(args.warmup):
-            e2e_step(k)
+            one[k % POOL].replay()
         torch.cuda.synchronize(dev)
         et_sync = 0.0
         for k in range(args.steps):
             a = torch.cuda.Event(enable_timing=True)
             b = torch.cuda.Event(enable_timing=True)
             a.record(stream)
-            e2e_step(args.warmup + k)
+            one[(args.warmup + k) % POOL].replay()
             b.record(stream)
             torch.cuda.synchronize(dev)
             et_sync += a.elapsed_time(b)
         et_sync = allreduce_max(et_sync, world, dev)
 
-        # (2) a stream of images: two input / output buffer pairs, the copies on
-        # their own streams, so that image k+1 is copied in and image k-1 out
-        # while image k is processed (every image still makes both copies)
+        # (2) a stream of images, software-pipelined over two buffer pairs:
+        # the replay for image k runs its step on pair k % 2 while, on two
+        # other streams inside the same graph, image k+1 is copied into the
+        # other pair and image k-1's outputs are copied out of it (each
+        # image still makes both copies; the last image's copy-out follows
+        # the loop, inside the timed region)
         inbuf2 = torch.empty_like(inbuf)
         outbuf2 = torch.empty_like(outbuf)
-        x2, f2 = inbuf2[:nx].view(plan.sx), inbuf2[nx:nx + nf].view((K,) + plan.sf)
-        y2 = inbuf2[nx + nf:].view(plan.sy)
-        gx2 = outbuf2[:nx * 4].view(torch.float32).view(plan.sx)
-        gf2 = outbuf2[nx * 4:(nx + nf) * 4].view(torch.float32).view((K,) + plan.sf)
-        loss2 = outbuf2[o_loss:].view(torch.float64).view(())
-        inbuf2.copy_(inbuf)
-        graph2 = torch.cuda.CUDAGraph()
-        with torch.cuda.graph(graph2, stream=stream):
-            plan.loss_grad(x2, f2, y2, loss=loss2, gx=gx2, gf=gf2)
-        torch.cuda.synchronize(dev)
-        bufs = [(inbuf, outbuf, graph), (inbuf2, outbuf2, graph2)]
+        pairs = [(inbuf, outbuf), (inbuf2, outbuf2)]
         houts = [hout, torch.empty_like(hout).pin_memory()]
-        s_in = torch.cuda.Stream(device=dev)
-        s_out = torch.cuda.Stream(device=dev)
-        ev_in = [torch.cuda.Event(), torch.cuda.Event()]
-        ev_comp = [torch.cuda.Event(), torch.cuda.Event()]
-        ev_out = [torch.cuda.Event(), torch.cuda.Event()]
-        for e in ev_comp + ev_out:
-            e.record(stream)
 
-        def pipelined(k0, n):
-            for k in range(k0, k0 + n):
-                i = k % 2
-                ib, ob, gph = bufs[i]
+        def pair_step(i):
+            ib, ob = pairs[i]
+            plan.loss_grad(ib[:nx].view(plan.sx), ib[nx:nx + nf].view((K,) + plan.sf), ib[nx + nf:].view(plan.sy),
+                           loss=ob[o_loss:].view(torch.float64).view(()),
+                           gx=ob[:nx * 4].view(torch.float32).view(plan.sx),
+                           gf=ob[nx * 4:(nx + nf) * 4].view(torch.float32).view((K,) + plan.sf))
+
+        POOLE = POOL + POOL % 2  # even, so that image k's pair is k % 2 for every replay
+        piped = []
+        for k in range(POOLE):
+            i = k % 2
+            gp = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(gp, stream=stream):
+                s_in.wait_stream(stream)
+                s_out.wait_stream(stream)
                 with torch.cuda.stream(s_in):
-                    s_in.wait_event(ev_comp[i])  # image k-2 has been read
-                    ib.copy_(hins[k % POOL], non_blocking=True)
-                    ev_in[i].record(s_in)
-                stream.wait_event(ev_in[i])
-                stream.wait_event(ev_out[i])  # image k-2's outputs have been copied out
-                gph.replay()
-                ev_comp[i].record(stream)
+                    pairs[1 - i][0].copy_(hins[(k + 1) % POOL], non_blocking=True)
                 with torch.cuda.stream(s_out):
-                    s_out.wait_event(ev_comp[i])
-                    houts[i].copy_(ob, non_blocking=True)
-                    ev_out[i].record(s_out)
+                    houts[1 - i].copy_(pairs[1 - i][1], non_blocking=True)
+                pair_step(i)
+                stream.wait_stream(s_in)
+                stream.wait_stream(s_out)
+            piped.append(gp)
+        torch.cuda.synchronize(dev)
 
-        pipelined(0, max(args.warmup, 4))
+        def pipelined(n):
+            inbuf.copy_(hins[0], non_blocking=True)
+            for k in range(n):
+                piped[k % POOLE].replay()
+            houts[(n - 1) % 2].copy_(pairs[(n - 1) % 2][1], non_blocking=True)
+
+        pipelined(max(args.warmup, 4))
         torch.cuda.synchronize(dev)
         a = torch.cuda.Event(enable_timing=True)
         b = torch.cuda.Event(enable_timing=True)
-        a.record(s_in)
-        pipelined(0, args.steps)
-        b.record(s_out)
+        a.record(stream)
+        pipelined(args.steps)
+        b.record(stream)
         torch.cuda.synchronize(dev)
         et = allreduce_max(a.elapsed_time(b), world, dev)
     h2d = hins[0].numel() * 4
@@ -397,7 +417,7 @@ def run_ours(args, rank, world, dev):
     plan.forward_both(x, f, out=y, xhat_out=xhat, fhat_out=fhat)
     torch.cuda.synchronize(dev)
     return dict(plan=plan, wa=wa, w=w, x_np=x_np, f_np=f_np, y_obs=y_obs.cpu().numpy(),
-                gx=gx.cpu().numpy(), gf=gf.cpu().numpy(), y=y.cpu().numpy(), t_ms=t_ms,
+                gx=gx.cpu().numpy(), gf=gf.cpu().numpy(), y=y.cpu().numpy(), t_ms=t_ms, t_events=t_events,
                 kern_ms=kern_ms, unfused_ms=unfused_ms, e2e_ms=et, e2e_sync_ms=et_sync, h2d=h2d, d2h=d2h, clocks=clk,
                 det_ms=det_ms,
                 t_flushed=t_flushed, pool=POOL)
@@ -405,12 +425,14 @@ def run_ours(args, rank, world, dev):
 
 def kernel_times(plan, sets, r, xhat, fhat, gx, gf, loss, stream, dev, reps):
     """Device time each kernel adds to the graph-captured step: the step's own
-    sequence (memset of the residual, the fused residual forward clearing the
-    adjoint's accumulators as a side job, the fused adjoint) captured as three
-    prefixes -- the memset, memset + forward, the whole step -- for every input
-    set, replayed in turn (inputs not in L2, as for the timed steps) and timed
-    with CUDA events; forward = T(memset + forward) - T(memset), adjoint =
-    T(step) - T(memset + forward).  Each includes its launch gap in the graph."""
+    sequence (the clear of the residual, which the fused residual forward
+    overlaps; the forward, clearing the adjoint's accumulators as a side job;
+    the fused adjoint) captured as prefixes -- the clear + forward, the whole
+    step -- beside a one-node graph (a memset of the residual: the launch cost
+    every graph pays), for every input set, replayed in turn (inputs not in L2,
+    as for the timed steps) and timed with CUDA events; forward =
+    T(clear + forward) - T(one node), adjoint = T(step) - T(clear + forward).
+    Each includes its launch gap in the graph."""
     import ctypes
     import torch
     from vmbd_gb300 import _lib
@@ -420,10 +442,12 @@ def kernel_times(plan, sets, r, xhat, fhat, gx, gf, loss, stream, dev, reps):
     nx = int(np.prod(plan.sx))
 
     def seq(n, x, f, y_obs):
-        r.zero_()
+        if n == 0:
+            r.zero_()  # a graph of one node: the launch cost the others share
         if n >= 1:
+            # the step's clear of the residual (a zero kernel) and its forward
             _lib.check(L.eff_forward_both_ex(plan._h, _ptr(x), _ptr(f), _ptr(y_obs), _ptr(r), _ptr(xhat),
-                                             _ptr(fhat), _lib.OUT_ZEROED, _ptr(gx), nx, _ptr(loss), 1, 1, st))
+                                             _ptr(fhat), 0, _ptr(gx), nx, _ptr(loss), 1, 1, st))
         if n >= 2:
             _lib.check(L.eff_adjoint_ex(plan._h, _ptr(r), None, None, _ptr(fhat), _ptr(xhat), _ptr(gx), _ptr(gf),
                                         _ptr(loss), _lib.ADJ_EXACT,
@@ -453,8 +477,9 @@ def kernel_times(plan, sets, r, xhat, fhat, gx, gf, loss, stream, dev, reps):
                 if i >= np_:
                     tot[n] += a.elapsed_time(b)
     t = [v / reps for v in tot]
-    return {"forward": t[1] - t[0], "adjoint": t[2] - t[1], "memset": t[0],
-            "how": "differences of graph-replayed prefixes of the step (memset | + forward | + adjoint), "
+    return {"forward": t[1] - t[0], "adjoint": t[2] - t[1], "graph_one_node": t[0],
+            "how": "differences of graph-replayed prefixes of the step (one-node graph | clear + forward | "
+                   "+ adjoint), "
                    "input sets rotated"}
 
 
@@ -967,18 +992,24 @@ def main():
                 "ms_per_step": e2e_ms, "h2d_bytes_per_step": R["h2d"], "d2h_bytes_per_step": R["d2h"],
                 "inputs": f"{R['pool']} distinct pinned host input sets, rotated",
                 "how": "a stream of images: each image copied in, processed and copied out, the copies of "
-                       "neighbouring images overlapping the step (two buffer pairs, copy streams)",
+                       "neighbouring images overlapping the step (two buffer pairs, copy streams); copies and "
+                       "step captured in one CUDA graph per image, replayed in turn",
                 "one_at_a_time": {"value": world * pixels / (e2e_sync_ms * 1e-3) / 1e6, "ms_per_step": e2e_sync_ms,
-                                  "how": "copy in, step, copy out, then the next image"}},
+                                  "how": "copy in, step, copy out (one graph), then the next image"}},
+        "per_step_events": {"value": world * pixels / (R["t_events"] / args.steps * 1e-3) / 1e6,
+                            "ms_per_step": R["t_events"] / args.steps,
+                            "what": "the same timed steps, each step's own event interval summed (charges "
+                                    "every replay's launch latency; value is the back-to-back loop)"},
         "l2_flushed": {"value": world * pixels / (R["t_flushed"] * 1e-3) / 1e6, "ms_per_step": R["t_flushed"],
                        "what": "the same step with a 256 MB write before it (inputs and the kernels' code "
-                               "read from HBM)"},
+                               "read from HBM; per-step event intervals)"},
         "input_sets": R["pool"],
-        "deterministic": ({"ms_per_step": R["det_ms"], "vs_atomic": R["det_ms"] / ms,
+        "deterministic": ({"ms_per_step": R["det_ms"], "vs_atomic": R["det_ms"] / R["t_flushed"],
                            "what": "same step on a plan with the fixed-order gather overlap-add (bit-identical "
-                                   "repeats): forward + gather + adjoint + gather"}
+                                   "repeats): forward + gather + adjoint + gather; L2 flushed before each "
+                                   "step, against l2_flushed"}
                           if isinstance(R["det_ms"], float) else {"error": R["det_ms"]}),
-        "gpu_launches": 2 * args.steps,
+        "gpu_launches": 3 * args.steps,  # per step: the residual's clear, the forward, the adjoint
         "clocks": clk,
     }
     if rank == 0 and world == 1:

@@ -56,7 +56,7 @@ extern "C" {
 #define EFF_MODE_SAME 1
 #define EFF_MODE_FULL 2
 
-#define EFF_OUT_ZEROED 1 /* flags: the call's accumulated output is already zero (no memset) */
+#define EFF_OUT_ZEROED 1 /* flags: the call's accumulated output is already zero (no clear) */
 #define EFF_LOSS_OF_Y 2  /* eff_adjoint_ex flags: y is already a residual; loss += 0.5 * sum y^2 */
 #define EFF_AFTER_FORWARD 4 /* eff_adjoint_ex flags: the call directly follows, on the same stream,
                                the forward call that produced its inputs; its kernel may be
@@ -224,10 +224,12 @@ EFF_API int eff_deconv_xdirect(const EffPlan* plan, const float* y, const void* 
 EFF_API int eff_adjoint_masked(const EffPlan* plan, const float* y, const float* mask, const void* fhat,
                        const void* xhat, float* gx, float* gf, int adj_mode, int batch, void* stream);
 
-/* Chained calls without memsets.  Loops that run many forward / adjoint
- * pairs in one graph (the MFBD frame) spend ~1 us per memset node; these
- * let each accumulated output be zeroed as a side job of an earlier kernel
- * that does not touch it, and its own call skip the memset.
+/* Chained calls without clears.  A call whose output is accumulated first
+ * clears it with a small kernel that the call's own kernel overlaps (about
+ * 1 us in a graph); loops that run many forward / adjoint pairs in one graph
+ * (the MFBD frame) can instead have each accumulated output zeroed as a side
+ * job of an earlier kernel that does not touch it, and its own call skip
+ * the clear.
  * eff_forward_ex: eff_forward_image (operand EFF_OPERAND_IMAGE, spec =
  *   fhat) or eff_forward_psf (EFF_OPERAND_PSF, spec = xhat); sub
  *   (nullable, not aliasing y): y = EFF - sub, the residual against an
@@ -250,7 +252,7 @@ EFF_API int eff_adjoint_ex(const EffPlan* plan, const float* y, const float* y_o
                    void* stream);
 /* eff_forward_both (sub NULL) / eff_forward_residual (sub = y_obs, not
  * aliasing y) with the same flags and side jobs as eff_forward_ex.
- * eff_loss_grad is: memset of its residual buffer, this call with
+ * eff_loss_grad is: a clear of its residual buffer, this call with
  * EFF_OUT_ZEROED clearing gx and loss, eff_adjoint_ex with
  * EFF_OUT_ZEROED | EFF_LOSS_OF_Y. */
 EFF_API int eff_forward_both_ex(const EffPlan* plan, const float* x, const float* f, const float* sub, float* y,

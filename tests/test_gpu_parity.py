@@ -490,3 +490,42 @@ def test_chained_call_entry_points(cuda):
                                 _lib.ADJ_EXACT, _lib.AFTER_FORWARD, 1, st))
     gx_plain, _ = plan.adjoint(res, fh, xh, want_psf=False)
     assert rel(gx_pdl.cpu(), gx_plain.cpu()) < 1e-6
+
+
+def test_cleared_outputs_at_unaligned_offsets(cuda):
+    """Accumulated outputs are cleared by a small kernel (4-byte words up to
+    the first 16-byte boundary, 16-byte stores, 4-byte words after the last)
+    that the operator's kernel overlaps: outputs starting 4, 8 and 12 bytes
+    past a boundary, in buffers full of garbage, get the results of fresh
+    aligned ones, and nothing outside them is written."""
+    import torch
+    from vmbd_gb300.eff import EffPlan
+    wa, g, x, f, r = make(**CASES["cfg1_literal"])
+    plan = EffPlan(wa, g.sf, g.mode, device=cuda)
+    xt, ft, rt = t(x, cuda), t(f, cuda), t(r, cuda)
+    fh, xh = plan.psf_spectrum(ft), plan.image_spectrum(xt)
+    yo = 0.5 * rt
+    y_ref = plan.forward_image(xt, fh)
+    loss_ref, gx_ref, _ = plan.adjoint_residual(rt, yo, fh, xh, want_psf=False)
+    u_ref, _ = plan.deconv_xdirect(rt, fhat=fh, alpha=0.01, beta=0.01)
+    ny, nx = int(np.prod(plan.sy)), int(np.prod(plan.sx))
+    for off in (1, 2, 3):
+        buf = torch.full((ny + 8,), 7.0, device=cuda)
+        y = buf[off:off + ny].view(plan.sy)
+        plan.forward_image(xt, fh, out=y)
+        assert rel(y.cpu(), y_ref.cpu()) < 1e-6
+        assert bool((buf[:off] == 7.0).all()) and bool((buf[off + ny:] == 7.0).all())
+        gbuf = torch.full((nx + 8,), 3.0, device=cuda)
+        gx = gbuf[off:off + nx].view(plan.sx)
+        lbuf = torch.full((4,), 5.0, dtype=torch.float64, device=cuda)
+        loss = lbuf[off]
+        plan.adjoint_residual(rt, yo, fh, xh, want_psf=False, gx=gx, loss=loss)
+        assert rel(gx.cpu(), gx_ref.cpu()) < 1e-6
+        assert bool((gbuf[:off] == 3.0).all()) and bool((gbuf[off + nx:] == 3.0).all())
+        assert abs(float(loss) - float(loss_ref)) < 1e-6 * float(loss_ref)
+        assert int((lbuf == 5.0).sum()) == 3
+        ubuf = torch.full((nx + 8,), 9.0, device=cuda)
+        u = ubuf[off:off + nx].view(plan.sx)
+        plan.deconv_xdirect(rt, fhat=fh, alpha=0.01, beta=0.01, u=u)
+        assert rel(u.cpu(), u_ref.cpu()) < 1e-6
+        assert bool((ubuf[:off] == 9.0).all()) and bool((ubuf[off + nx:] == 9.0).all())

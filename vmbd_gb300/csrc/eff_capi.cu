@@ -3,7 +3,7 @@
 // Plan creation validates the geometry as OlaGPU.__init__ does
 // (olaGPU.py:95-168), uploads the separable window factors and the FP64-built
 // twiddle table, and picks the FFT frame.  The compute entry points only
-// enqueue work on the caller's stream (memset of atomically accumulated
+// enqueue work on the caller's stream (a clear of atomically accumulated
 // outputs + one kernel) and allocate nothing.
 #include <algorithm>
 #include <atomic>
@@ -140,11 +140,24 @@ bool deterministic_ola(const EffPlan* p, int op, const eff::Params& P) {
   return false;
 }
 
-// Clear an output the kernels accumulate into (a deterministic plan's
-// outputs are stored whole by the gather instead: nothing to clear).
-cudaError_t clear_output(const EffPlan* p, void* ptr, size_t bytes, cudaStream_t st) {
-  if (p->det) return cudaSuccess;
-  return cudaMemsetAsync(ptr, 0, bytes, st);
+// Clear the outputs the kernel described by P accumulates into (a and b,
+// nullable) with the zero kernel, and launch that kernel right behind it
+// (P.pdl = 2): its transforms run beside the clear, and it waits for the
+// clear before its output phase.  Saves the separate memset's dependency
+// (about 2 us per call in a captured graph).  A deterministic plan stores
+// its outputs whole: nothing to clear.
+int clear_before(const EffPlan* p, eff::Params& P, void* a, size_t abytes, void* b, size_t bbytes,
+                 cudaStream_t st) {
+  if (p->det || (!a && !b)) return EFF_OK;
+  eff::ZeroArgs Z;
+  Z.p[0] = a;
+  Z.bytes[0] = a ? (long long)abytes : 0;
+  Z.p[1] = b;
+  Z.bytes[1] = b ? (long long)bbytes : 0;
+  cudaError_t e = eff::launch_zero(Z, p->num_sms, st);
+  if (e != cudaSuccess) return cuda_fail(e, "clearing an output");
+  P.pdl = 2;
+  return EFF_OK;
 }
 
 // The parameters of image b of a batch, for a launch over that image alone.
@@ -297,13 +310,9 @@ int adjoint_impl(const EffPlan* plan, const float* y, const float* y_obs, const 
     P.hi1 = plan->off[1] + plan->g.sw[1] < plan->E[1] ? plan->off[1] + plan->g.sw[1] : plan->E[1];
   }
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  if (gx && !zeroed) {
-    cudaError_t e = clear_output(plan, gx, sizeof(float) * P.x_bs * batch, st);
-    if (e != cudaSuccess) return cuda_fail(e, "clearing an output");
-  }
-  if (loss && !zeroed) {
-    cudaError_t e = clear_output(plan, loss, sizeof(double) * batch, st);
-    if (e != cudaSuccess) return cuda_fail(e, "clearing an output");
+  if (!zeroed) {
+    if (int s = clear_before(plan, P, gx, sizeof(float) * P.x_bs * batch, loss, sizeof(double) * batch, st))
+      return s;
   }
   return run(plan, eff::OP_ADJ, P, batch, stream);
 }
@@ -355,8 +364,8 @@ int loss_grad_impl(const EffPlan* plan, const float* x, const float* f, const fl
   P.zero_nf = gx ? P.x_bs * batch : 0;
   P.zero_d = loss;
   P.zero_nd = loss ? batch : 0;
-  cudaError_t e = clear_output(plan, y, sizeof(float) * P.y_bs * batch, static_cast<cudaStream_t>(stream));
-  if (e != cudaSuccess) return cuda_fail(e, "clearing an output");
+  if (int s = clear_before(plan, P, y, sizeof(float) * P.y_bs * batch, nullptr, 0, static_cast<cudaStream_t>(stream)))
+    return s;
   int s = run(plan, eff::OP_FWD_BOTH, P, batch, stream);
   if (s != EFF_OK) return s;
   // the adjoint may be scheduled while the forward runs (it waits for it)
@@ -619,8 +628,8 @@ int eff_forward_image(const EffPlan* plan, const float* x, const void* fhat, flo
   P.out0 = y;
   P.out0_bs = P.y_bs;
   P.a_out = static_cast<float2*>(xhat_out);
-  cudaError_t e = clear_output(plan, y, sizeof(float) * P.y_bs * batch, static_cast<cudaStream_t>(stream));
-  if (e != cudaSuccess) return cuda_fail(e, "clearing an output");
+  if (int s = clear_before(plan, P, y, sizeof(float) * P.y_bs * batch, nullptr, 0, static_cast<cudaStream_t>(stream)))
+    return s;
   return run(plan, eff::OP_FWD_IMAGE, P, batch, stream);
 }
 
@@ -634,8 +643,8 @@ int eff_forward_psf(const EffPlan* plan, const float* f, const void* xhat, float
   P.out0 = y;
   P.out0_bs = P.y_bs;
   P.a_out = static_cast<float2*>(fhat_out);
-  cudaError_t e = clear_output(plan, y, sizeof(float) * P.y_bs * batch, static_cast<cudaStream_t>(stream));
-  if (e != cudaSuccess) return cuda_fail(e, "clearing an output");
+  if (int s = clear_before(plan, P, y, sizeof(float) * P.y_bs * batch, nullptr, 0, static_cast<cudaStream_t>(stream)))
+    return s;
   return run(plan, eff::OP_FWD_PSF, P, batch, stream);
 }
 
@@ -661,8 +670,8 @@ int eff_forward_ex(const EffPlan* plan, int operand, const float* u, const void*
   P.zero_d = zero_nd > 0 ? zero_d : nullptr;
   P.zero_nd = zero_nd;
   if (!(flags & EFF_OUT_ZEROED)) {
-    cudaError_t e = clear_output(plan, y, sizeof(float) * P.y_bs * batch, static_cast<cudaStream_t>(stream));
-    if (e != cudaSuccess) return cuda_fail(e, "clearing an output");
+    if (int s = clear_before(plan, P, y, sizeof(float) * P.y_bs * batch, nullptr, 0, static_cast<cudaStream_t>(stream)))
+      return s;
   }
   return run(plan, operand == EFF_OPERAND_IMAGE ? eff::OP_FWD_IMAGE : eff::OP_FWD_PSF, P, batch, stream);
 }
@@ -711,11 +720,8 @@ int eff_deconv_xdirect(const EffPlan* plan, const float* y, const void* fhat, co
   P.lo1 = plan->off[1];
   P.alpha = alpha;
   P.beta = beta;
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
-  if (u) {
-    cudaError_t e = clear_output(plan, u, sizeof(float) * P.x_bs * batch, st);
-    if (e != cudaSuccess) return cuda_fail(e, "clearing an output");
-  }
+  if (int s = clear_before(plan, P, u, sizeof(float) * P.x_bs * batch, nullptr, 0, static_cast<cudaStream_t>(stream)))
+    return s;
   return run(plan, eff::OP_DECONV, P, batch, stream);
 }
 
@@ -736,8 +742,8 @@ int eff_forward_both(const EffPlan* plan, const float* x, const float* f, float*
   P.out0_bs = P.y_bs;
   P.a_out = static_cast<float2*>(xhat_out);
   P.b_out = static_cast<float2*>(fhat_out);
-  cudaError_t e = clear_output(plan, y, sizeof(float) * P.y_bs * batch, static_cast<cudaStream_t>(stream));
-  if (e != cudaSuccess) return cuda_fail(e, "clearing an output");
+  if (int s = clear_before(plan, P, y, sizeof(float) * P.y_bs * batch, nullptr, 0, static_cast<cudaStream_t>(stream)))
+    return s;
   return run(plan, eff::OP_FWD_BOTH, P, batch, stream);
 }
 
@@ -756,8 +762,8 @@ int eff_forward_residual(const EffPlan* plan, const float* x, const float* f, co
   P.pf = reinterpret_cast<const char*>(y_obs);
   P.pf_bytes = (long long)sizeof(float) * P.y_bs;
   P.sub = y_obs;
-  cudaError_t e = clear_output(plan, r, sizeof(float) * P.y_bs * batch, static_cast<cudaStream_t>(stream));
-  if (e != cudaSuccess) return cuda_fail(e, "clearing an output");
+  if (int s = clear_before(plan, P, r, sizeof(float) * P.y_bs * batch, nullptr, 0, static_cast<cudaStream_t>(stream)))
+    return s;
   return run(plan, eff::OP_FWD_BOTH, P, batch, stream);
 }
 
@@ -786,8 +792,8 @@ int eff_forward_both_ex(const EffPlan* plan, const float* x, const float* f, con
   P.zero_d = zero_nd > 0 ? zero_d : nullptr;
   P.zero_nd = zero_nd;
   if (!(flags & EFF_OUT_ZEROED)) {
-    cudaError_t e = clear_output(plan, y, sizeof(float) * P.y_bs * batch, static_cast<cudaStream_t>(stream));
-    if (e != cudaSuccess) return cuda_fail(e, "clearing an output");
+    if (int s = clear_before(plan, P, y, sizeof(float) * P.y_bs * batch, nullptr, 0, static_cast<cudaStream_t>(stream)))
+      return s;
   }
   return run(plan, eff::OP_FWD_BOTH, P, batch, stream);
 }

@@ -85,8 +85,10 @@ struct Params {
                            //   tiles + (b K + k) * tile size, instead of adding it into the image;
                            //   ola_gather sums the tiles in a fixed order
   double* loss_part;       // deterministic loss: each CTA stores its share at loss_part[b ncta + cta]
-  int pdl;                 // launched with programmatic stream serialization right after the
-                           //   kernel whose results it reads: wait (griddepcontrol.wait) first
+  int pdl;                 // launched with programmatic stream serialization: 1 = right after
+                           //   the kernel whose results it reads, wait (griddepcontrol.wait)
+                           //   first; 2 = right after the zero kernel clearing its accumulated
+                           //   outputs, wait before the output phase
 };
 
 // TMA bulk prefetch of a contiguous range into L2 (16-byte aligned start and
@@ -706,7 +708,7 @@ __device__ __forceinline__ void eff_patch(const Params& P, int k, long long b, f
   // visible, before it reads anything that kernel wrote.
   if constexpr (OP == OP_FWD_BOTH || OP == OP_FWD_IMAGE || OP == OP_FWD_PSF)
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-  if (P.pdl) asm volatile("griddepcontrol.wait;" ::: "memory");
+  if (P.pdl == 1) asm volatile("griddepcontrol.wait;" ::: "memory");
   if constexpr (!kRegTw)
     for (int i = tid; i < N; i += blockDim.x) tw_s[i] = __ldg(P.tw + i);
   if (nst && tid == 0) mbar_init(sbar, 1);
@@ -881,6 +883,8 @@ __device__ __forceinline__ void eff_patch(const Params& P, int k, long long b, f
     return;
   }
   phase_sync();
+  // the outputs this phase accumulates into are cleared by the kernel before
+  if (P.pdl == 2) asm volatile("griddepcontrol.wait;" ::: "memory");
 
   // Phase 3: inverse row transforms and epilogues.
   if constexpr (OP == OP_FWD_IMAGE || OP == OP_FWD_PSF || OP == OP_FWD_BOTH) {

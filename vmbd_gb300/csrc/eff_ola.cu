@@ -52,4 +52,44 @@ cudaError_t launch_ola_gather(const GatherArgs& A, int num_sms, cudaStream_t st)
   return cudaGetLastError();
 }
 
+// Clear of an output that the next kernel accumulates into.  Each block
+// triggers the dependent launch first: the clear then runs beside that
+// kernel's transforms, which only need the output at their end.
+__global__ void __launch_bounds__(256) zero_kernel(ZeroArgs Z) {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  const long long t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long nt = (long long)gridDim.x * blockDim.x;
+#pragma unroll 1
+  for (int r = 0; r < 2; ++r) {
+    char* p = static_cast<char*>(Z.p[r]);
+    const long long n = Z.bytes[r];
+    if (!p || n <= 0) continue;
+    // 4-byte words up to the first 16-byte boundary, 16-byte stores, then words
+    long long head = (long long)((16 - (reinterpret_cast<unsigned long long>(p) & 15ull)) & 15ull);
+    if (head > n) head = n;
+    const long long n16 = (n - head) >> 4;
+    const long long tail0 = head + (n16 << 4);
+    if (t0 < head / 4) reinterpret_cast<unsigned*>(p)[t0] = 0u;
+    uint4* q = reinterpret_cast<uint4*>(p + head);
+    for (long long i = t0; i < n16; i += nt) q[i] = make_uint4(0u, 0u, 0u, 0u);
+    const long long ntail = (n - tail0) / 4;
+    if (t0 < ntail) reinterpret_cast<unsigned*>(p + tail0)[t0] = 0u;
+  }
+}
+
+cudaError_t launch_zero(const ZeroArgs& Z, int num_sms, cudaStream_t st) {
+  long long n16 = 0;
+  for (int r = 0; r < 2; ++r) {
+    if (Z.p[r] && ((reinterpret_cast<unsigned long long>(Z.p[r]) & 3ull) || (Z.bytes[r] & 3)))
+      return cudaErrorInvalidValue;
+    if (Z.p[r] && Z.bytes[r] > 0) n16 = n16 > Z.bytes[r] / 16 ? n16 : Z.bytes[r] / 16;
+  }
+  long long blocks = (n16 + 255) / 256;
+  const long long cap = num_sms > 0 ? num_sms : 1;
+  if (blocks > cap) blocks = cap;
+  if (blocks < 1) blocks = 1;
+  zero_kernel<<<(unsigned)blocks, 256, 0, st>>>(Z);
+  return cudaGetLastError();
+}
+
 }  // namespace eff

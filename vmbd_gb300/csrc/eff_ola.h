@@ -19,4 +19,17 @@ struct GatherArgs {
 
 cudaError_t launch_ola_gather(const GatherArgs& A, int num_sms, cudaStream_t st);
 
+// Up to two byte ranges to clear (4-byte aligned, sizes multiples of 4;
+// nullptr / 0 for an unused range).
+struct ZeroArgs {
+  void* p[2];
+  long long bytes[2];
+};
+
+// Clears the ranges with a kernel whose blocks let the next kernel on the
+// stream start at once, when that one is launched with programmatic stream
+// serialization; that kernel waits (griddepcontrol.wait) before its first
+// access to the ranges, so the clear overlaps its start.
+cudaError_t launch_zero(const ZeroArgs& Z, int num_sms, cudaStream_t st);
+
 }  // namespace eff

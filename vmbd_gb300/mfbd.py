@@ -103,7 +103,7 @@ class OnlineMFBD:
     # The frame's stages, in the order frame() runs them (each only enqueues
     # work on the current stream).  Accumulated outputs are cleared as side
     # jobs of earlier kernels that do not touch them (EFF_OUT_ZEROED on their
-    # own call), so the frame graph has three memset nodes instead of ~40.
+    # own call), so the frame graph has three clears instead of ~40.
     def begin_frame(self, y: torch.Tensor = None) -> None:
         """Edgetaper of y, the saturation mask, the X object of x."""
         if y is not None:
@@ -123,7 +123,7 @@ class OnlineMFBD:
         OZ = _lib.OUT_ZEROED
         amode = _lib.ADJ_EXACT if self.adjoint == "exact" else _lib.ADJ_REFERENCE
         # residual X f - y into y_pred (cleared by the previous PSF step;
-        # memset at k = 0); side jobs: clear dots (and yg at k = 0)
+        # cleared by the call at k = 0); side jobs: clear dots (and yg at k = 0)
         self._check(L.eff_forward_ex(P._h, _lib.OPERAND_PSF, _ptr(self.f), _ptr(self.xhat), _ptr(self.ypred),
                                      _ptr(self.y), None, OZ if k > 0 else 0, _ptr(self.yg) if k == 0 else None,
                                      ny if k == 0 else 0, _ptr(self.dots), 3, 1, st))
@@ -177,8 +177,9 @@ class OnlineMFBD:
                                     0 if last else ny, st))
 
     def launches_per_frame(self) -> int:
-        """Kernels of this library one frame launches."""
-        return ((1 if self.taper else 0) + 1 + self.n_pg * 4 + 1 + 1 + 1 + 1 + self.n_mu * 4)
+        """Kernels of this library one frame launches (the two clears, of
+        the first forward's output and of the masked adjoint's, included)."""
+        return ((1 if self.taper else 0) + 1 + self.n_pg * 4 + 1 + 1 + 1 + 1 + self.n_mu * 4 + 2)
 
 
 def make_sequence(plan: EffPlan, n_frames: int, seed: int = 3, peak: float = 1000.0, sigma: float = 0.005):
