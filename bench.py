@@ -222,15 +222,10 @@ def run_ours(args, rank, world, dev):
         torch.cuda.synchronize(dev)
 
         def timed_graph(n, flushed=False):
-            """(sum of the steps' own event intervals, whole loop) in ms.
-            The whole loop -- n steps replayed back to back, as a job over a
-            stream of images runs them -- is the throughput figure; the sum
-            of per-step intervals also charges every replay's launch latency
-            (a loop that waits for each step's result sees about that)."""
+            """Sum of the steps' own event intervals in ms (each interval also
+            charges its replay's launch latency; a loop that waits for each
+            step's result sees about that)."""
             evs = []
-            a0 = torch.cuda.Event(enable_timing=True)
-            b0 = torch.cuda.Event(enable_timing=True)
-            a0.record(stream)
             for k in range(n):
                 if flushed:
                     flush.fill_(1.0)
@@ -240,26 +235,39 @@ def run_ours(args, rank, world, dev):
                 (graph if flushed else graphs[k % POOL]).replay()
                 b.record(stream)
                 evs.append((a, b))
+            torch.cuda.synchronize(dev)
+            return sum(a.elapsed_time(b) for a, b in evs)
+
+        def timed_loop(n):
+            """n steps replayed back to back between two events, in ms: the
+            throughput of a job over a stream of images (the host only issues
+            one replay per step, so it stays ahead of the device)."""
+            a0 = torch.cuda.Event(enable_timing=True)
+            b0 = torch.cuda.Event(enable_timing=True)
+            reps = [graphs[k % POOL].replay for k in range(n)]
+            a0.record(stream)
+            for r_ in reps:
+                r_()
             b0.record(stream)
             torch.cuda.synchronize(dev)
-            return sum(a.elapsed_time(b) for a, b in evs), a0.elapsed_time(b0)
+            return a0.elapsed_time(b0)
 
-        timed_graph(max(args.warmup, POOL))  # every set once, so that the timed steps see a steady state
+        timed_loop(max(args.warmup, POOL))  # every set once, so that the timed steps see a steady state
         clocks = Clocks(dev.index if dev.index is not None else 0)
         barrier(world)
         torch.cuda.synchronize(dev)
         clocks.start()
-        t_events, t_ms = timed_graph(args.steps)
+        t_ms = timed_loop(args.steps)
         torch.cuda.synchronize(dev)
         barrier(world)
         clk = clocks.stop()
         t_ms = allreduce_max(t_ms, world, dev)
-        t_events = allreduce_max(t_events, world, dev)
+        t_events = allreduce_max(timed_graph(args.steps), world, dev)
         # the same step with the L2 flushed before it (one set): data and the
         # kernels' code are then read from HBM (per-step intervals: the loop
         # also holds the flushes)
         timed_graph(args.warmup, flushed=True)
-        t_flushed = timed_graph(args.steps, flushed=True)[0] / args.steps
+        t_flushed = timed_graph(args.steps, flushed=True) / args.steps
 
         # per-kernel durations inside the step: differences of graph-captured
         # prefixes of the step's own sequence, input sets rotated
