@@ -337,6 +337,13 @@ EFF_API int eff_plan_device_errors(const EffPlan* plan, int* flags, int clear);
  * where a step's spectra sit in L2.  For all plans of the process. */
 EFF_API int eff_set_spectrum_staging(int on);
 
+/* 1 (default): kernels that read the image (image spectrum, forwards from x)
+ * copy each CTA's rows of the patch window into shared memory with one
+ * tensor-engine (TMA) copy at kernel start, where x is 16-byte aligned and
+ * the image width and the patch hop are multiples of 4; 0: every lane loads
+ * its own values.  For all plans of the process. */
+EFF_API int eff_set_image_tile(int on);
+
 /* Testing hook: overwrite the device a plan records as its own, so that a
  * test can check that calls on a mismatched device are refused before any
  * work is queued.  Not for production use. */

@@ -529,3 +529,42 @@ def test_cleared_outputs_at_unaligned_offsets(cuda):
         plan.deconv_xdirect(rt, fhat=fh, alpha=0.01, beta=0.01, u=u)
         assert rel(u.cpu(), u_ref.cpu()) < 1e-6
         assert bool((ubuf[:off] == 9.0).all()) and bool((ubuf[off + nx:] == 9.0).all())
+
+
+@pytest.mark.parametrize("name", ["cfg1_literal", "cfg2_literal", "cfg2_winaux"])
+def test_image_tile_copy_matches_lane_loads(cuda, name):
+    """Kernels reading the image either copy each CTA's rows of the patch
+    window into shared memory with one tensor-engine copy (x 16-byte
+    aligned, image width and hop multiples of 4) or load every value
+    themselves: the same values go through the same arithmetic, so the
+    results are bit-identical (batched launches included)."""
+    import torch
+    from vmbd_gb300 import _lib
+    from vmbd_gb300.eff import EffPlan
+    L = _lib.load()
+    spec = dict(CASES[name])
+    wa, g, x, f, r = make(**spec)
+    plan = EffPlan(wa, g.sf, g.mode, device=cuda)
+    xs = np.stack([x, x[::-1].copy()])
+    xt, ft, xbt = t(x, cuda), t(f, cuda), t(xs, cuda)
+    fh = plan.psf_spectrum(ft)
+    out = {}
+    try:
+        for on in (0, 1):
+            _lib.check(L.eff_set_image_tile(on), L)
+            xh = plan.empty_spectrum()
+            y = plan.forward_image(xt, fh, xhat_out=xh)
+            xh2, fh2 = plan.empty_spectrum(), plan.empty_spectrum()
+            y2 = plan.forward_both(xt, ft, xhat_out=xh2, fhat_out=fh2)
+            xs_h = plan.image_spectrum(xbt)
+            out[on] = [v.cpu() for v in (y, xh, y2, xh2, xs_h)]
+    finally:
+        _lib.check(L.eff_set_image_tile(1), L)
+    for a, b in zip(out[0], out[1]):
+        # forwards overlap-add with atomics (order may differ): 1e-6; spectra exact
+        if a.is_complex():
+            assert torch.equal(a, b)
+        else:
+            assert rel(a.numpy(), b.numpy()) < 1e-6
+    assert rel(out[1][0].numpy(), eff64.forward(x, f, g, wa.ws.astype(np.float64))) < TOL
+    assert plan.device_errors() == 0

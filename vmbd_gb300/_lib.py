@@ -38,7 +38,7 @@ EXPORTS = (
     "eff_set_cluster_mode", "eff_batch_create", "eff_batch_destroy", "eff_batch_items",
     "eff_batch_forward_both", "eff_batch_adjoint_residual", "eff_deconv_xdirect", "eff_forward_ex",
     "eff_adjoint_ex", "eff_forward_residual", "eff_batch_forward_residual", "eff_test_plan_set_device",
-    "eff_forward_both_ex", "eff_plan_device_errors", "eff_set_spectrum_staging",
+    "eff_forward_both_ex", "eff_plan_device_errors", "eff_set_spectrum_staging", "eff_set_image_tile",
 )
 
 
@@ -121,6 +121,7 @@ def _bind(L: ctypes.CDLL) -> ctypes.CDLL:
         "eff_test_plan_set_device": ([vp, ip], ip),
         "eff_plan_device_errors": ([vp, ctypes.POINTER(ctypes.c_int), ip], ip),
         "eff_set_spectrum_staging": ([ip], ip),
+        "eff_set_image_tile": ([ip], ip),
         "eff_batch_create": ([vp, vp, ip, ctypes.POINTER(vp)], ip),
         "eff_batch_destroy": ([vp], ip),
         "eff_batch_items": ([vp], ip),

@@ -63,6 +63,10 @@ thread_local std::string g_last_error;
 constexpr size_t kSmemLimit = 227u * 1024u;
 // 0: choose per call; 1: one CTA per patch; 2: a 2-CTA cluster per patch.
 std::atomic<int> g_cluster_mode{0};
+// 1 (default): kernels whose first operand is the image copy each CTA's rows
+// of the patch window into shared memory with one tensor-engine copy where
+// the geometry allows (see image_tile); 0: every lane loads its values.
+std::atomic<int> g_image_tile{1};
 // 1: stage cached spectra in shared memory where they fit; 0 (default): read
 // them from global memory (L2-resident in a step; measured faster on the
 // 512^2 step: adjoint 19.4 vs 21.6 us).
@@ -111,14 +115,14 @@ eff::Params base_params(const EffPlan* p) {
 }
 
 int launch_kernel(const EffPlan* p, int op, const eff::Params& P, int batch, int CL, int threads, size_t smem,
-                  cudaStream_t st) {
+                  cudaStream_t st, const CUtensorMap* xmap = nullptr) {
   cudaError_t e;
   switch (p->N) {
-    case 64: e = eff::launch_n64(op, CL, P, p->K, batch, threads, smem, st); break;
-    case 128: e = eff::launch_n128(op, CL, P, p->K, batch, threads, smem, st); break;
-    case 192: e = eff::launch_n192(op, CL, P, p->K, batch, threads, smem, st); break;
-    case 256: e = eff::launch_n256(op, CL, P, p->K, batch, threads, smem, st); break;
-    case 512: e = eff::launch_n512(op, CL, P, p->K, batch, threads, smem, st); break;
+    case 64: e = eff::launch_n64(op, CL, P, p->K, batch, threads, smem, st, xmap); break;
+    case 128: e = eff::launch_n128(op, CL, P, p->K, batch, threads, smem, st, xmap); break;
+    case 192: e = eff::launch_n192(op, CL, P, p->K, batch, threads, smem, st, xmap); break;
+    case 256: e = eff::launch_n256(op, CL, P, p->K, batch, threads, smem, st, xmap); break;
+    case 512: e = eff::launch_n512(op, CL, P, p->K, batch, threads, smem, st, xmap); break;
     default: return fail(EFF_ERR_UNSUPPORTED, "frame size");
   }
   if (e != cudaSuccess)
@@ -227,6 +231,57 @@ int run_deterministic(const EffPlan* p, int op, const eff::Params& P, int batch,
   return EFF_OK;
 }
 
+// cuTensorMapEncodeTiled, looked up once through the runtime (no link
+// dependency on the driver library).
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = []() -> EncodeTiledFn {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      f = nullptr;
+    (void)cudaGetLastError();
+    return reinterpret_cast<EncodeTiledFn>(f);
+  }();
+  return fn;
+}
+
+// The image tile of kernels whose operand A is the image: a tensor map over
+// x as [batch][sx0][sx1] floats and, in P, the box each CTA copies (tile_w
+// columns: sw1 rounded up to 4; tile_rows: the rows of the image units one
+// CTA transforms -- 2 NG of them when the cluster takes all units in one
+// round, else the whole window).  Only where the copy is well formed: x
+// 16-byte aligned, image rows and the patch hop multiples of 4 floats (so
+// that every box starts on a 16-byte boundary), box sides <= 256.  False:
+// the kernel loads its values itself.
+bool image_tile(const EffPlan* p, int op, eff::Params& P, int batch, int CL, int threads, CUtensorMap* map) {
+  P.tile_rows = P.tile_w = 0;
+  if (!g_image_tile.load() || eff::opnd_a(op) != eff::OPND_IMAGE || !P.x || p->det) return false;
+  const EffGeom& g = p->g;
+  if ((reinterpret_cast<unsigned long long>(P.x) & 15ull) || (g.sx[1] & 3) || (g.hop[1] & 3)) return false;
+  const int G = p->N / eff::lane_values(p->N), NG = threads / G, NW = CL * NG;
+  const int nA = (g.sw[0] + 1) / 2;
+  const int rows = (CL > 1 && nA <= NW) ? std::min(2 * NG, eff::even_up(g.sw[0])) : eff::even_up(g.sw[0]);
+  const int w = (g.sw[1] + 3) & ~3;
+  if (rows > 256 || w > 256) return false;
+  EncodeTiledFn enc = encode_tiled();
+  if (!enc) return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)g.sx[1], (cuuint64_t)g.sx[0], (cuuint64_t)batch};
+  const cuuint64_t strides[2] = {(cuuint64_t)g.sx[1] * sizeof(float), (cuuint64_t)g.sx[0] * g.sx[1] * sizeof(float)};
+  const cuuint32_t box[3] = {(cuuint32_t)w, (cuuint32_t)rows, 1};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  if (enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(P.x), dims, strides, box, estr,
+          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return false;
+  P.tile_rows = rows;
+  P.tile_w = w;
+  return true;
+}
+
 int run(const EffPlan* p, int op, const eff::Params& P0, int batch, void* stream) {
   eff::Params P = P0;
   P.stage_spec = 0;
@@ -249,12 +304,15 @@ int run(const EffPlan* p, int op, const eff::Params& P0, int batch, void* stream
     P.stage_spec = 1;
     if (eff::smem_bytes(p->N, op, P, threads, CL) > kSmemLimit || !g_stage_spectra.load()) P.stage_spec = 0;
   }
+  CUtensorMap xmap;
+  const bool tile = image_tile(p, op, P, batch, CL, threads, &xmap);
+  if (tile && eff::smem_bytes(p->N, op, P, threads, CL) > kSmemLimit) P.tile_rows = P.tile_w = 0;
   const size_t smem = eff::smem_bytes(p->N, op, P, threads, CL);
   if (smem > kSmemLimit)
     return fail(EFF_ERR_UNSUPPORTED, "frame needs " + std::to_string(smem) + " bytes of shared memory");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   if (deterministic_ola(p, op, P)) return run_deterministic(p, op, P, batch, CL, threads, smem, st);
-  return launch_kernel(p, op, P, batch, CL, threads, smem, st);
+  return launch_kernel(p, op, P, batch, CL, threads, smem, st, P.tile_rows > 0 ? &xmap : nullptr);
 }
 
 // The plan's tables live on the device that was current at eff_plan_create;
@@ -888,6 +946,12 @@ int eff_plan_device_errors(const EffPlan* plan, int* flags, int clear) {
   if (e == cudaSuccess) e = cudaMemcpy(flags, plan->err, sizeof(int), cudaMemcpyDeviceToHost);
   if (e == cudaSuccess && clear) e = cudaMemset(plan->err, 0, sizeof(int));
   if (e != cudaSuccess) return cuda_fail(e, "reading the device error word");
+  return EFF_OK;
+}
+
+int eff_set_image_tile(int on) {
+  if (on != 0 && on != 1) return fail(EFF_ERR_INVALID, "image tile must be 0 or 1");
+  g_image_tile.store(on);
   return EFF_OK;
 }
 

@@ -8,9 +8,15 @@
 #include "../../include/vmbd_eff.h"
 
 namespace eff {
-cudaError_t launch_n192(int, int, const Params&, int, int, int, size_t, cudaStream_t) { return cudaErrorNotSupported; }
-cudaError_t launch_n256(int, int, const Params&, int, int, int, size_t, cudaStream_t) { return cudaErrorNotSupported; }
-cudaError_t launch_n512(int, int, const Params&, int, int, int, size_t, cudaStream_t) { return cudaErrorNotSupported; }
+cudaError_t launch_n192(int, int, const Params&, int, int, int, size_t, cudaStream_t, const CUtensorMap*) {
+  return cudaErrorNotSupported;
+}
+cudaError_t launch_n256(int, int, const Params&, int, int, int, size_t, cudaStream_t, const CUtensorMap*) {
+  return cudaErrorNotSupported;
+}
+cudaError_t launch_n512(int, int, const Params&, int, int, int, size_t, cudaStream_t, const CUtensorMap*) {
+  return cudaErrorNotSupported;
+}
 }  // namespace eff
 
 extern "C" {

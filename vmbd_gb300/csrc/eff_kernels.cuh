@@ -27,6 +27,7 @@
 // Reference semantics: OlaGPU.cnv / OlaGPU.cnvtp, olaGPU.py:170-311.
 #pragma once
 #include <cooperative_groups.h>
+#include <cuda.h>  // CUtensorMap (the type only; maps are encoded on the host)
 
 #include "eff_fft.cuh"
 
@@ -85,6 +86,9 @@ struct Params {
                            //   tiles + (b K + k) * tile size, instead of adding it into the image;
                            //   ola_gather sums the tiles in a fixed order
   double* loss_part;       // deterministic loss: each CTA stores its share at loss_part[b ncta + cta]
+  int tile_rows, tile_w;   // image operand by the tensor engine (tile_rows > 0, kernels given a
+                           //   tensor map of x): a tile_rows x tile_w box of the patch's window
+                           //   per CTA into shared memory at kernel start (zero outside the image)
   int pdl;                 // launched with programmatic stream serialization: 1 = right after
                            //   the kernel whose results it reads, wait (griddepcontrol.wait)
                            //   first; 2 = right after the zero kernel clearing its accumulated
@@ -114,6 +118,16 @@ __device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, unsign
                    smem_addr(dst)),
                "l"(src), "r"(bytes), "r"(smem_addr(bar))
                : "memory");
+}
+// Box at (c0, c1, c2) of a rank-3 tensor map -> this CTA's shared memory
+// (128-byte aligned), counted on bar.  c0 * 4 bytes must be a multiple of 16.
+__device__ __forceinline__ void tensor_copy_3d(void* dst, const CUtensorMap* map, int c0, int c1, int c2,
+                                               unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+      "[%5];" ::"r"(smem_addr(dst)),
+      "l"(reinterpret_cast<unsigned long long>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(smem_addr(bar))
+      : "memory");
 }
 __device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
   unsigned ok;
@@ -194,6 +208,12 @@ __host__ __device__ inline int staged_specs(const Params& P, int op) {
   return 0;
 }
 __host__ __device__ constexpr int staged_cols(int N, int CL) { return N / (2 * CL) + 1; }
+// Shared memory (float2) of the image tile: up to 15 slots to a 128-byte
+// boundary, the tile, the mbarrier.
+__host__ __device__ inline int image_tile_f2(const Params& P, int op) {
+  if (opnd_a(op) != OPND_IMAGE || P.tile_rows <= 0) return 0;
+  return 15 + (P.tile_rows * P.tile_w + 1) / 2 + 1;
+}
 
 template <int N>
 __device__ __forceinline__ unsigned group_mask(int lane) {
@@ -321,10 +341,34 @@ __device__ __forceinline__ void load_resid_rows(const Params& P, const Patch& T,
 // valid column range are taken once per row pair.
 template <int N>
 __device__ __forceinline__ void load_image_rows(const Params& P, const Patch& T, int ra, int g,
-                                                float2 (&v)[FftShape<N>::R]) {
+                                                float2 (&v)[FftShape<N>::R], const float* tile = nullptr,
+                                                int t_r0 = 0) {
   constexpr int G = FftShape<N>::G;
   constexpr int R = FftShape<N>::R;
   const int i0 = T.m * P.hop0 + ra;
+  // rows of this CTA's image tile (shared memory): the same values, one
+  // shared-memory read each
+  if (tile && ra >= t_r0 && ra + 1 < t_r0 + P.tile_rows) {
+    const bool okA = ra < P.sw0 && i0 < P.sx0;
+    const bool okB = ra + 1 < P.sw0 && i0 + 1 < P.sx0;
+    const float2 wa = okA ? __ldg(P.win0 + T.m * P.sw0 + ra) : make_float2(0.f, 0.f);
+    const float2 wb = okB ? __ldg(P.win0 + T.m * P.sw0 + ra + 1) : make_float2(0.f, 0.f);
+    const int chi = min(P.sw1, P.sx1 - T.n * P.hop1);
+    const float* ta = tile + (ra - t_r0) * P.tile_w;
+    const float2* w1 = P.win1 + T.n * P.sw1;
+#pragma unroll
+    for (int mm = 0; mm < R; ++mm) {
+      const int c = g + G * mm;
+      float a = 0.f, b = 0.f;
+      if (c < chi && EFF_IN(c, P.tile_w, P.err)) {
+        const float2 wc = __ldg(w1 + c);
+        if (okA) a = window_weight(wa, wc) * ta[c];
+        if (okB) b = window_weight(wb, wc) * ta[P.tile_w + c];
+      }
+      v[mm] = make_float2(a, b);
+    }
+    return;
+  }
   const bool okA = ra < P.sw0 && i0 < P.sx0;
   const bool okB = ra + 1 < P.sw0 && i0 + 1 < P.sx0;
   const bool okW = !(okA || okB) || EFF_IN(T.m * P.sw0 + ra + (okB ? 1 : 0), P.csf0 * P.sw0, P.err);
@@ -352,7 +396,8 @@ __device__ __forceinline__ void load_image_rows(const Params& P, const Patch& T,
 // Operand rows (ra, ra+1) packed as re/im, layout A.
 template <int N, int KIND>
 __device__ __forceinline__ void load_rows(const Params& P, const Patch& T, int ra, int g,
-                                          float2 (&v)[FftShape<N>::R]) {
+                                          float2 (&v)[FftShape<N>::R], const float* tile = nullptr,
+                                          int t_r0 = 0) {
   constexpr int G = FftShape<N>::G;
   constexpr int R = FftShape<N>::R;
   if constexpr (KIND == OPND_RESID) {
@@ -361,7 +406,7 @@ __device__ __forceinline__ void load_rows(const Params& P, const Patch& T, int r
     else if (!T.y_obs) load_resid_rows<N, false, true>(P, T, ra, g, v);
     else load_resid_rows<N, true, true>(P, T, ra, g, v);
   } else if constexpr (KIND == OPND_IMAGE) {
-    load_image_rows<N>(P, T, ra, g, v);
+    load_image_rows<N>(P, T, ra, g, v, tile, t_r0);
   } else {
 #pragma unroll
     for (int mm = 0; mm < R; ++mm) {
@@ -620,7 +665,7 @@ __device__ __forceinline__ void dc_product_split(const float2 (&s)[FftShape<N>::
 // (and of the peer) must call it with the same arguments.
 template <int N, int OP, int CL>
 __device__ __forceinline__ void eff_patch(const Params& P, int k, long long b, float2* smem, int cta,
-                                          int ncta) {
+                                          int ncta, const CUtensorMap* xmap = nullptr) {
   constexpr int G = FftShape<N>::G;
   constexpr int R = FftShape<N>::R;
   constexpr int A = opnd_a(OP);
@@ -687,6 +732,22 @@ __device__ __forceinline__ void eff_patch(const Params& P, int k, long long b, f
   float2* stage = stash + 2 * N;
   stage += (reinterpret_cast<unsigned long long>(stage) & 15ull) ? 1 : 0;
   unsigned long long* sbar = reinterpret_cast<unsigned long long*>(stage + nst * SC * SP);
+  // Image tile (operand A = image, a tensor map given): rows [t_r0, t_r0 +
+  // tile_rows) of the patch's window -- the rows of the image units this CTA
+  // transforms (one round over the cluster: CTA c's 2 NG rows from 2 c NG;
+  // else all of them) -- copied by the tensor engine at kernel start.
+  float* xtile = nullptr;
+  unsigned long long* tbar = nullptr;
+  int t_r0 = 0;
+  if constexpr (A == OPND_IMAGE) {
+    if (xmap && P.tile_rows > 0) {
+      unsigned long long a = reinterpret_cast<unsigned long long>(stage + nst * SC * SP + (nst ? 1 : 0));
+      a = (a + 127ull) & ~127ull;
+      xtile = reinterpret_cast<float*>(a);
+      tbar = reinterpret_cast<unsigned long long*>(xtile + ((P.tile_rows * P.tile_w + 1) & ~1));
+      t_r0 = P.tile_rows >= even_up(P.sw0) ? 0 : 2 * F.rank * NG;
+    }
+  }
 
   // Twiddles: R = 8 (frames 64 and 128) -- this lane's R factors
   // W_N^{g k1} in registers, loaded here with no barrier before the first
@@ -712,7 +773,12 @@ __device__ __forceinline__ void eff_patch(const Params& P, int k, long long b, f
   if constexpr (!kRegTw)
     for (int i = tid; i < N; i += blockDim.x) tw_s[i] = __ldg(P.tw + i);
   if (nst && tid == 0) mbar_init(sbar, 1);
-  if (!kRegTw || nst) __syncthreads();  // the twiddle table / the mbarrier, before the first use
+  if (tbar && tid == 0) {
+    mbar_init(tbar, 1);
+    mbar_expect_tx(tbar, (unsigned)(P.tile_rows * P.tile_w * sizeof(float)));
+    tensor_copy_3d(xtile, xmap, T.n * P.hop1, T.m * P.hop0 + t_r0, (int)b, tbar);
+  }
+  if (!kRegTw || nst || tbar) __syncthreads();  // the twiddle table / the mbarriers, before the first use
   // Cached spectra this CTA multiplies by in the column pass: its columns of
   // each, copied into shared memory by the bulk-copy engine while the row
   // pass runs (one column per copy, into padded slots).
@@ -773,13 +839,21 @@ __device__ __forceinline__ void eff_patch(const Params& P, int k, long long b, f
     // (one loop, so that the transform code exists once: every thread takes
     // the first iteration and meets the barrier there)
     bool first = true;
+    bool tile_waited = false;
 #pragma unroll 1
     for (int u = wid;; u += NW) {
       float2 v[R], p[R];
       int row = -1;
       if (u < nA + nB) {
         if (u < nA) {
-          load_rows<N, A>(P, T, 2 * u, g, v);
+          if (tbar && !tile_waited) {
+            tile_waited = true;
+            if (!mbar_wait_bounded(tbar, 0)) {
+              atomicOr(P.err, kErrCopyTimeout);
+              xtile = nullptr;  // this thread reads global memory instead
+            }
+          }
+          load_rows<N, A>(P, T, 2 * u, g, v, xtile, t_r0);
           row = 2 * u;
         } else {
           load_rows<N, OPND_PSF>(P, T, 2 * (u - nA), g, v);
@@ -797,6 +871,8 @@ __device__ __forceinline__ void eff_patch(const Params& P, int k, long long b, f
       if (row < 0) break;
       r2c_scatter<N, CL>(v, p, F, row, g);
     }
+    // every thread sees the tile copy complete before the CTA can end
+    if (tbar && !tile_waited && !mbar_wait_bounded(tbar, 0)) atomicOr(P.err, kErrCopyTimeout);
   }
   phase_sync();
 
@@ -1074,10 +1150,11 @@ __device__ __forceinline__ void zero_next(const Params& P) {
 
 // One patch per CTA (CL = 1) or per 2-CTA cluster, images along blockIdx.y.
 template <int N, int OP, int CL>
-__global__ void __launch_bounds__(max_threads(N)) eff_kernel(Params P) {
-  extern __shared__ __align__(16) float2 smem[];
+__global__ void __launch_bounds__(max_threads(N))
+    eff_kernel(const __grid_constant__ Params P, const __grid_constant__ CUtensorMap xmap) {
+  extern __shared__ __align__(128) float2 smem[];
   if constexpr (OP == OP_FWD_BOTH || OP == OP_FWD_IMAGE || OP == OP_FWD_PSF) zero_next(P);
-  eff_patch<N, OP, CL>(P, blockIdx.x / CL, blockIdx.y, smem, blockIdx.x, gridDim.x);
+  eff_patch<N, OP, CL>(P, blockIdx.x / CL, blockIdx.y, smem, blockIdx.x, gridDim.x, P.tile_rows > 0 ? &xmap : nullptr);
 }
 
 }  // namespace eff

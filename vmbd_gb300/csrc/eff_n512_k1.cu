@@ -2,7 +2,7 @@
 #include "eff_launch.cuh"
 
 namespace eff {
-template cudaError_t launch_one<512, 0, 4>(const Params&, int, int, int, size_t, cudaStream_t);
-template cudaError_t launch_one<512, 1, 4>(const Params&, int, int, int, size_t, cudaStream_t);
-template cudaError_t launch_one<512, 2, 4>(const Params&, int, int, int, size_t, cudaStream_t);
+template cudaError_t launch_one<512, 0, 4>(const Params&, int, int, int, size_t, cudaStream_t, const CUtensorMap*);
+template cudaError_t launch_one<512, 1, 4>(const Params&, int, int, int, size_t, cudaStream_t, const CUtensorMap*);
+template cudaError_t launch_one<512, 2, 4>(const Params&, int, int, int, size_t, cudaStream_t, const CUtensorMap*);
 }  // namespace eff

@@ -2,6 +2,6 @@
 #include "eff_launch.cuh"
 
 namespace eff {
-template cudaError_t launch_one<512, 3, 4>(const Params&, int, int, int, size_t, cudaStream_t);
-template cudaError_t launch_one<512, 4, 4>(const Params&, int, int, int, size_t, cudaStream_t);
+template cudaError_t launch_one<512, 3, 4>(const Params&, int, int, int, size_t, cudaStream_t, const CUtensorMap*);
+template cudaError_t launch_one<512, 4, 4>(const Params&, int, int, int, size_t, cudaStream_t, const CUtensorMap*);
 }  // namespace eff

@@ -2,6 +2,6 @@
 #include "eff_launch.cuh"
 
 namespace eff {
-template cudaError_t launch_one<512, 5, 8>(const Params&, int, int, int, size_t, cudaStream_t);
-template cudaError_t launch_one<512, 6, 8>(const Params&, int, int, int, size_t, cudaStream_t);
+template cudaError_t launch_one<512, 5, 8>(const Params&, int, int, int, size_t, cudaStream_t, const CUtensorMap*);
+template cudaError_t launch_one<512, 6, 8>(const Params&, int, int, int, size_t, cudaStream_t, const CUtensorMap*);
 }  // namespace eff
