@@ -433,14 +433,16 @@ def run_ours(args, rank, world, dev):
 
 def kernel_times(plan, sets, r, xhat, fhat, gx, gf, loss, stream, dev, reps):
     """Device time each kernel adds to the graph-captured step: the step's own
-    sequence (the clear of the residual, which the fused residual forward
-    overlaps; the forward, clearing the adjoint's accumulators as a side job;
-    the fused adjoint) captured as prefixes -- the clear + forward, the whole
-    step -- beside a one-node graph (a memset of the residual: the launch cost
-    every graph pays), for every input set, replayed in turn (inputs not in L2,
-    as for the timed steps) and timed with CUDA events; forward =
-    T(clear + forward) - T(one node), adjoint = T(step) - T(clear + forward).
-    Each includes its launch gap in the graph."""
+    sequence (the zero kernel clearing the residual, which the fused residual
+    forward overlaps; the forward, clearing the adjoint's accumulators as a
+    side job; the fused adjoint) captured as prefixes -- clear + forward, the
+    whole step -- beside the forward alone (its output taken as already
+    cleared: timing only) and a one-node graph (a memset of the residual: the
+    launch cost every graph pays), for every input set, replayed in turn
+    (inputs not in L2, as for the timed steps) and timed with CUDA events:
+    forward = T(forward) - T(one node), clear = T(clear + forward) -
+    T(forward), adjoint = T(step) - T(clear + forward).  Each includes its
+    launch gap in the graph."""
     import ctypes
     import torch
     from vmbd_gb300 import _lib
@@ -452,18 +454,20 @@ def kernel_times(plan, sets, r, xhat, fhat, gx, gf, loss, stream, dev, reps):
     def seq(n, x, f, y_obs):
         if n == 0:
             r.zero_()  # a graph of one node: the launch cost the others share
-        if n >= 1:
-            # the step's clear of the residual (a zero kernel) and its forward
+        if n in (1, 2, 3):
+            # n = 1, 2: the step's clear of the residual (a zero kernel) and
+            # its forward; n = 3: the forward alone
             _lib.check(L.eff_forward_both_ex(plan._h, _ptr(x), _ptr(f), _ptr(y_obs), _ptr(r), _ptr(xhat),
-                                             _ptr(fhat), 0, _ptr(gx), nx, _ptr(loss), 1, 1, st))
-        if n >= 2:
+                                             _ptr(fhat), _lib.OUT_ZEROED if n == 3 else 0, _ptr(gx), nx,
+                                             _ptr(loss), 1, 1, st))
+        if n == 2:
             _lib.check(L.eff_adjoint_ex(plan._h, _ptr(r), None, None, _ptr(fhat), _ptr(xhat), _ptr(gx), _ptr(gf),
                                         _ptr(loss), _lib.ADJ_EXACT,
                                         _lib.OUT_ZEROED | _lib.LOSS_OF_Y | _lib.AFTER_FORWARD, 1, st))
 
-    graphs = [[], [], []]
+    graphs = [[], [], [], []]
     with torch.cuda.stream(stream):
-        for n in range(3):
+        for n in range(4):
             seq(n, *sets[0])
             torch.cuda.synchronize(dev)
             for xs in sets:
@@ -472,10 +476,10 @@ def kernel_times(plan, sets, r, xhat, fhat, gx, gf, loss, stream, dev, reps):
                     seq(n, *xs)
                 graphs[n].append(gph)
         torch.cuda.synchronize(dev)
-        tot = [0.0, 0.0, 0.0]
+        tot = [0.0, 0.0, 0.0, 0.0]
         np_ = len(sets)
         for i in range(np_ + reps):
-            for n in range(3):  # interleaved, so that all three see the same conditions
+            for n in range(4):  # interleaved, so that all four see the same conditions
                 a = torch.cuda.Event(enable_timing=True)
                 b = torch.cuda.Event(enable_timing=True)
                 a.record(stream)
@@ -485,10 +489,9 @@ def kernel_times(plan, sets, r, xhat, fhat, gx, gf, loss, stream, dev, reps):
                 if i >= np_:
                     tot[n] += a.elapsed_time(b)
     t = [v / reps for v in tot]
-    return {"forward": t[1] - t[0], "adjoint": t[2] - t[1], "graph_one_node": t[0],
-            "how": "differences of graph-replayed prefixes of the step (one-node graph | clear + forward | "
-                   "+ adjoint), "
-                   "input sets rotated"}
+    return {"forward": t[3] - t[0], "clear": t[1] - t[3], "adjoint": t[2] - t[1], "graph_one_node": t[0],
+            "how": "differences of graph-replayed prefixes of the step (one-node graph | forward alone | "
+                   "clear + forward | + adjoint), input sets rotated"}
 
 
 def profile_run(args, dev):
