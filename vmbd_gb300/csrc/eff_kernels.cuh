@@ -239,7 +239,12 @@ struct Frame {
     return CL == 1 ? b : (b == N / 2 ? W : b - (b / W) * W);
   }
   __device__ __forceinline__ float2* at(int row, int b) const {
-    return part[owner(b)] + row * HP + lcol(b);
+    // CL = 2, frames up to 128: a select, so that the two pointers stay in
+    // registers (an index into part[] puts the array in local memory and
+    // adds a dependent load to every frame access; the frame-256 kernels
+    // have no registers to spare for it: their forward spills more)
+    if constexpr (CL == 2 && N <= 128) return (owner(b) ? part[1] : part[0]) + row * HP + lcol(b);
+    else return part[owner(b)] + row * HP + lcol(b);
   }
   static constexpr int kDcN = W;  // local column of bin N/2 (CTA 0; the DC unit packs it with column 0)
 };
