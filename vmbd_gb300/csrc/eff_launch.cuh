@@ -7,7 +7,8 @@
 namespace eff {
 
 // Shared-memory bytes of one CTA: twiddles + frame (its share of the columns)
-// + per-group exchange scratch + the DC unit's stash (2N); with staged
+// + per-group exchange scratch + the DC unit's stash (2N) + the row-owned
+// output block and its mbarrier (frame-128 pairs); with staged
 // spectra (P.stage_spec) also an alignment slot, the staged columns and the
 // mbarrier; with an image tile (P.tile_rows) the tile, its alignment and its
 // mbarrier.
@@ -15,7 +16,7 @@ inline size_t smem_bytes(int N, int op, const Params& P, int threads, int CL) {
   const int R = lane_values(N), G = N / R;
   const int scr = group_scratch(N);
   size_t n = (size_t)N + (size_t)frame_rows(P, op) * frame_pitch(N, CL) + (size_t)(threads / G) * scr +
-             2 * (size_t)N;
+             2 * (size_t)N + (size_t)out_rows_f2(P, op, N, CL);
   if (const int nst = staged_specs(P, op)) n += 1 + (size_t)nst * staged_cols(N, CL) * (N + kSpecPad) + 1;
   n += (size_t)image_tile_f2(P, op);
   return sizeof(float2) * n;
