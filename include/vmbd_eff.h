@@ -330,11 +330,13 @@ EFF_API int eff_set_cluster_mode(int mode);
 #define EFF_DEVERR_COPY_TIMEOUT 1
 EFF_API int eff_plan_device_errors(const EffPlan* plan, int* flags, int clear);
 
-/* 1: kernels that multiply by cached spectra (adjoints, forwards from a
- * cached spectrum, deconvolution) copy their columns of the spectra into
+/* Kernels that multiply by cached spectra (adjoints, forwards from a cached
+ * spectrum, deconvolution) either copy their columns of the spectra into
  * shared memory with the bulk-copy engine at kernel start, where the CTA's
- * shared memory allows; 0 (default): they read them from global memory,
- * where a step's spectra sit in L2.  For all plans of the process. */
+ * shared memory allows, or read them from global memory.  2 (default): the
+ * deconvolution copies (its spectra usually come from HBM), the rest read (a
+ * loss/gradient step's adjoint finds its spectra in L2); 1: every such
+ * kernel copies; 0: none does.  For all plans of the process. */
 EFF_API int eff_set_spectrum_staging(int on);
 
 /* 1 (default): kernels that read the image (image spectrum, forwards from x)

@@ -71,7 +71,7 @@ def test_operator_fixtures_in_bounds(cuda, dlib, path, cl, staging, det):
         assert plan.device_errors() == 0
     finally:
         _lib.check(dlib.eff_set_cluster_mode(0))
-        _lib.check(dlib.eff_set_spectrum_staging(0))
+        _lib.check(dlib.eff_set_spectrum_staging(2))  # the default
 
 
 @pytest.mark.parametrize("path", fixtures.deconv_paths(), ids=lambda p: os.path.basename(p))

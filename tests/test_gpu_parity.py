@@ -125,7 +125,7 @@ def cluster_mode(request, cuda):
     _lib.check(lib.eff_set_spectrum_staging(staging))
     yield mode
     _lib.check(lib.eff_set_cluster_mode(0))
-    _lib.check(lib.eff_set_spectrum_staging(0))
+    _lib.check(lib.eff_set_spectrum_staging(2))  # the default
 
 
 @pytest.mark.parametrize("name", list(CASES))

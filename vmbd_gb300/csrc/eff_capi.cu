@@ -67,10 +67,13 @@ std::atomic<int> g_cluster_mode{0};
 // of the patch window into shared memory with one tensor-engine copy where
 // the geometry allows (see image_tile); 0: every lane loads its values.
 std::atomic<int> g_image_tile{1};
-// 1: stage cached spectra in shared memory where they fit; 0 (default): read
-// them from global memory (L2-resident in a step; measured faster on the
-// 512^2 step: adjoint 19.4 vs 21.6 us).
-std::atomic<int> g_stage_spectra{0};
+// Cached spectra staged in shared memory (bulk copies at kernel start,
+// where they fit) or read from global memory: 2 (default) staged for the
+// deconvolution only, whose spectra usually come from HBM (512^2: 22.5 vs
+// 25.6 us), read for the rest -- a loss/gradient step's adjoint finds its
+// spectra in L2, just written by the forward (step 35.7 vs 36.8 us
+// staged); 1 staged for every kernel that multiplies by one; 0 never.
+std::atomic<int> g_stage_spectra{2};
 
 int fail(int code, const std::string& msg) {
   g_last_error = msg;
@@ -302,7 +305,10 @@ int run(const EffPlan* p, int op, const eff::Params& P0, int batch, void* stream
   // shared memory where that still fits.
   if (op == eff::OP_ADJ || op == eff::OP_FWD_IMAGE || op == eff::OP_FWD_PSF || op == eff::OP_DECONV) {
     P.stage_spec = 1;
-    if (eff::smem_bytes(p->N, op, P, threads, CL) > kSmemLimit || !g_stage_spectra.load()) P.stage_spec = 0;
+    const int mode = g_stage_spectra.load();
+    if (eff::smem_bytes(p->N, op, P, threads, CL) > kSmemLimit || mode == 0 ||
+        (mode == 2 && op != eff::OP_DECONV))
+      P.stage_spec = 0;
   }
   CUtensorMap xmap;
   const bool tile = image_tile(p, op, P, batch, CL, threads, &xmap);
@@ -956,7 +962,7 @@ int eff_set_image_tile(int on) {
 }
 
 int eff_set_spectrum_staging(int on) {
-  if (on != 0 && on != 1) return fail(EFF_ERR_INVALID, "spectrum staging must be 0 or 1");
+  if (on < 0 || on > 2) return fail(EFF_ERR_INVALID, "spectrum staging must be 0, 1 or 2");
   g_stage_spectra.store(on);
   return EFF_OK;
 }
