@@ -1006,6 +1006,50 @@ __device__ __forceinline__ void eff_patch(const Params& P, int k, long long b, f
   }
   phase_sync();
 
+  // This thread's part of the CTA's share of 0.5 ||r||^2 (adjoint with a
+  // loss): a contiguous range of pixels per CTA, whole float4s when both
+  // planes are 16-byte aligned.
+  auto loss_share = [&]() -> float {
+    const long long npx = (long long)P.sy0 * P.sy1;
+    const bool vec =
+        ((reinterpret_cast<unsigned long long>(T.y) | reinterpret_cast<unsigned long long>(T.y_obs)) & 15ull) == 0;
+    const long long chunk = vec ? ((npx + ncta - 1) / ncta + 3) & ~3LL : (npx + ncta - 1) / ncta;
+    const long long p0 = min(npx, (long long)cta * chunk);
+    const long long p1 = min(npx, p0 + chunk);
+    const long long q1 = vec ? p0 + ((p1 - p0) & ~3LL) : p0;
+    float acc = 0.f;
+    const float4* y4 = reinterpret_cast<const float4*>(T.y + p0);
+    const float4* o4 = reinterpret_cast<const float4*>(T.y_obs + p0);
+    if (T.y_obs) {
+      for (int q = tid; q < (int)((q1 - p0) >> 2); q += blockDim.x) {
+        const float4 a = __ldg(y4 + q), o = __ldg(o4 + q);
+        const float r0 = a.x - o.x, r1 = a.y - o.y, r2 = a.z - o.z, r3 = a.w - o.w;
+        acc = fmaf(r0, r0, acc);
+        acc = fmaf(r1, r1, acc);
+        acc = fmaf(r2, r2, acc);
+        acc = fmaf(r3, r3, acc);
+      }
+      for (long long p = q1 + tid; p < p1; p += blockDim.x) {
+        const float r = __ldg(T.y + p) - __ldg(T.y_obs + p);
+        acc = fmaf(r, r, acc);
+      }
+    } else {
+      for (int q = tid; q < (int)((q1 - p0) >> 2); q += blockDim.x) {
+        const float4 a = __ldg(y4 + q);
+        acc = fmaf(a.x, a.x, acc);
+        acc = fmaf(a.y, a.y, acc);
+        acc = fmaf(a.z, a.z, acc);
+        acc = fmaf(a.w, a.w, acc);
+      }
+      for (long long p = q1 + tid; p < p1; p += blockDim.x) {
+        const float r = __ldg(T.y + p);
+        acc = fmaf(r, r, acc);
+      }
+    }
+    return acc;
+  };
+  float loss_acc = 0.f;
+
   // Phase 2: column transforms, products, inverse column transforms (local).
   constexpr int kUnits = N / 2 / CL;  // column units this CTA owns
   // The bytes the peer's column units will store into this CTA's rows of the
@@ -1109,6 +1153,12 @@ __device__ __forceinline__ void eff_patch(const Params& P, int k, long long b, f
     // stores, counted on m3): no cluster barrier
     __syncthreads();
     if (O.U3 && !mbar_wait_bounded(m3, 0)) atomicOr(P.err, kErrCopyTimeout);
+  } else if constexpr (OP == OP_ADJ && CL > 1) {
+    // the loss share in the cluster barrier's wait: arrive once this CTA's
+    // columns are done, sum the share while the peer finishes, then wait
+    asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+    if (P.loss && (T.y_obs || P.loss_y)) loss_acc = loss_share();
+    asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
   } else {
     phase_sync();
   }
@@ -1238,47 +1288,11 @@ __device__ __forceinline__ void eff_patch(const Params& P, int k, long long b, f
       }
     }
   }
-  // Loss of the residual: this CTA's contiguous share of the pixels (after
-  // the transforms, when the observation is in L2).
+  // Loss of the residual: this CTA's share, summed during the barrier
+  // before phase 3 (cluster kernels) or here.
   if constexpr (OP == OP_ADJ) {
     if (P.loss && (T.y_obs || P.loss_y)) {
-      const long long npx = (long long)P.sy0 * P.sy1;
-      // shares of whole float4s when both planes are 16-byte aligned
-      const bool vec =
-          ((reinterpret_cast<unsigned long long>(T.y) | reinterpret_cast<unsigned long long>(T.y_obs)) & 15ull) == 0;
-      const long long chunk = vec ? ((npx + ncta - 1) / ncta + 3) & ~3LL : (npx + ncta - 1) / ncta;
-      const long long p0 = min(npx, (long long)cta * chunk);
-      const long long p1 = min(npx, p0 + chunk);
-      const long long q1 = vec ? p0 + ((p1 - p0) & ~3LL) : p0;
-      float acc = 0.f;
-      const float4* y4 = reinterpret_cast<const float4*>(T.y + p0);
-      const float4* o4 = reinterpret_cast<const float4*>(T.y_obs + p0);
-      if (T.y_obs) {
-        for (int q = tid; q < (int)((q1 - p0) >> 2); q += blockDim.x) {
-          const float4 a = __ldg(y4 + q), o = __ldg(o4 + q);
-          const float r0 = a.x - o.x, r1 = a.y - o.y, r2 = a.z - o.z, r3 = a.w - o.w;
-          acc = fmaf(r0, r0, acc);
-          acc = fmaf(r1, r1, acc);
-          acc = fmaf(r2, r2, acc);
-          acc = fmaf(r3, r3, acc);
-        }
-        for (long long p = q1 + tid; p < p1; p += blockDim.x) {
-          const float r = __ldg(T.y + p) - __ldg(T.y_obs + p);
-          acc = fmaf(r, r, acc);
-        }
-      } else {
-        for (int q = tid; q < (int)((q1 - p0) >> 2); q += blockDim.x) {
-          const float4 a = __ldg(y4 + q);
-          acc = fmaf(a.x, a.x, acc);
-          acc = fmaf(a.y, a.y, acc);
-          acc = fmaf(a.z, a.z, acc);
-          acc = fmaf(a.w, a.w, acc);
-        }
-        for (long long p = q1 + tid; p < p1; p += blockDim.x) {
-          const float r = __ldg(T.y + p);
-          acc = fmaf(r, r, acc);
-        }
-      }
+      const float acc = CL > 1 ? loss_acc : loss_share();
       double d = acc;
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
