@@ -124,6 +124,9 @@ def test_xdirect_plan_level_batch_and_both_outputs(cuda):
         u_ref = eff64.deconv_xdirect(ys[b].cpu().numpy(), eff64.psf_spectrum(fs[b].cpu().numpy(), g), g, ws,
                                      "image", 1e-2, 1e-2)
         assert rel(u[b].cpu(), u_ref) < TOL
+    # no wait in the kernels ran out (the row hand-off between the cluster's
+    # CTAs counts the bytes each single-output call sends)
+    assert plan.device_errors() == 0
 
 
 @pytest.mark.parametrize("cluster", [1, 2], ids=["cta", "cluster2"])
@@ -142,6 +145,7 @@ def test_xdirect_cluster_modes_agree(cuda, cluster):
     assert rel(u.cpu(), eff64.deconv_xdirect(y, eff64.psf_spectrum(f, g), g, ws, "image", 0.0, 1e-2)) < TOL
     fz_ref = eff64.deconv_xdirect(y, eff64.image_spectrum(x, g, ws), g, ws, "psf", 0.0, 1e-2)
     assert rel(fz.cpu(), fz_ref) < psf_tol(y, x, g, ws, 0.0, 1e-2, fz_ref)
+    assert plan.device_errors() == 0
 
 
 def test_direct_mode_matches_oracle(cuda):
