@@ -922,6 +922,11 @@ def main():
               "adjoint of r (loss, both gradients)", "images_per_gpu": 1,
               "l2": "inputs larger than L2: the timed steps rotate through distinct input sets of over twice the "
                     "L2 in total", "parallelism": f"replicas x{world}"}
+    if w.get("sw") and w.get("hop"):
+        cov = [(w["csf"][d] - 1) * w["hop"][d] + w["sw"][d] for d in range(2)]
+        if cov != list(w["sx"]):
+            config["pixels"] = (f"Mpixel/s counts the whole {w['sx'][0]}x{w['sx'][1]} image; this grid's patches "
+                                f"cover {cov[0]}x{cov[1]} of it (the reference arm counts the same way)")
 
     if args.impl == "reference":
         if rank != 0:
