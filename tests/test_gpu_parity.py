@@ -102,6 +102,12 @@ CASES = {
     "frame512_cl8": dict(sx=(600, 600), csf=(2, 2), sf=(25, 25), kind="motion"),
     "frame512_same": dict(sx=(400, 440), csf=(2, 2), sf=(25, 21), mode="same"),
     "full_mode_f192": dict(sx=(200, 232), csf=(3, 4), sf=(12, 10), mode="full", sfft=192),
+    # frame 128 with odd extents (E 113 x 106: the cluster's CTAs own 58 and 56
+    # rows of phase 3), an odd window height and a hop of 80 columns (the image
+    # tile by the tensor engine: rows of 101-row windows, 96 of 336 columns)
+    "tile_odd": dict(sx=(281, 336), csf=(3, 4), sf=(13, 11), sw=(101, 96), hop=(90, 80), kind="motion"),
+    "tile_odd_same": dict(sx=(281, 336), csf=(3, 4), sf=(13, 11), sw=(101, 96), hop=(90, 80), kind="motion",
+                          mode="same"),
     # frame 64 (extent 48 x 56): its CTAs have a spare warp for the DC column unit
     "frame64": dict(sx=(80, 96), csf=(3, 3), sf=(9, 9), kind="motion"),
     "frame64_same": dict(sx=(70, 90), csf=(3, 4), sf=(9, 7), mode="same"),
@@ -110,7 +116,7 @@ CASES = {
 FRAME = {"cfg1_literal": 128, "cfg1_winaux": 128, "cfg2_literal": 128, "cfg2_winaux": 256,
          "cfg2_winaux_f192": 192, "cfg3_winaux": 256, "cfg3_winaux_f192": 192, "cfg4_mixed": 256,
          "cfg4_mixed_f192": 192, "cfg1_literal_f192": 192, "frame512_cl4": 512, "frame512_cl8a": 512, "frame512_cl8": 512,
-         "frame512_same": 512, "frame64": 64, "frame64_same": 64}
+         "frame512_same": 512, "frame64": 64, "frame64_same": 64, "tile_odd": 128, "tile_odd_same": 128}
 
 
 @pytest.fixture(params=[(1, 0), (2, 0), (2, 1)], ids=["cta", "cluster2", "cluster2-staged-spectra"])
@@ -531,7 +537,7 @@ def test_cleared_outputs_at_unaligned_offsets(cuda):
         assert bool((ubuf[:off] == 9.0).all()) and bool((ubuf[off + nx:] == 9.0).all())
 
 
-@pytest.mark.parametrize("name", ["cfg1_literal", "cfg2_literal", "cfg2_winaux"])
+@pytest.mark.parametrize("name", ["cfg1_literal", "cfg2_literal", "cfg2_winaux", "tile_odd", "tile_odd_same"])
 def test_image_tile_copy_matches_lane_loads(cuda, name):
     """Kernels reading the image either copy each CTA's rows of the patch
     window into shared memory with one tensor-engine copy (x 16-byte
