@@ -17,6 +17,10 @@
 namespace eff {
 
 __global__ void __launch_bounds__(256) ola_gather_kernel(GatherArgs A) {
+  // launched with programmatic stream serialization: the kernel after it may
+  // be scheduled now, and this one waits for the kernel storing the tiles
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
   const long long n = (long long)A.rows * A.cols;
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
        p += (long long)gridDim.x * blockDim.x) {
@@ -48,7 +52,17 @@ cudaError_t launch_ola_gather(const GatherArgs& A, int num_sms, cudaStream_t st)
   const long long cap = 8LL * (num_sms > 0 ? num_sms : 1);
   if (blocks > cap) blocks = cap;
   if (blocks < 1) blocks = 1;
-  ola_gather_kernel<<<(unsigned)blocks, 256, 0, st>>>(A);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)blocks);
+  cfg.blockDim = dim3(256);
+  cfg.stream = st;
+  cudaLaunchAttribute attr;
+  attr.id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr.val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = &attr;
+  cfg.numAttrs = 1;
+  cudaError_t e = cudaLaunchKernelEx(&cfg, ola_gather_kernel, A);
+  if (e != cudaSuccess) return e;
   return cudaGetLastError();
 }
 
